@@ -1,0 +1,149 @@
+// cmc_common.cuh -- pieces shared by the sweep and evaluation kernels and by
+// the host layer: the random source, the shared-memory plan, the per-CTA view.
+//
+// The sweep they serve (cmc_sweep.cuh), in brief:
+//
+// Work decomposition on the GPU:
+//   * one thread-block CLUSTER per sequence iseq; its G CTAs own R = nbeta/G
+//     temperatures each (CTA rank c owns ibeta in [c*R, (c+1)*R));
+//   * thread r < R of a CTA owns replica r: its RNG state, its proposal,
+//     its Metropolis decision and its step-size adaptation;
+//   * every thread of the CTA evaluates the model for all R replicas over a
+//     strided share of the data; per-replica chi^2 partials are reduced with
+//     warp shuffles and a fixed-order shared-memory pass (deterministic);
+//   * the replica exchange of a sequence runs on cluster rank 0, thread 0,
+//     with the ibeta = 0 replica's generator, over chi^2 values gathered from
+//     the other CTAs through distributed shared memory; the winning
+//     permutation is then applied by every CTA pulling its new parameter
+//     rows from their owners (DSMEM), between cluster barriers.
+//
+// The algorithm is the reference's (src/gpu_mcmc.cu):
+//   init_rng :228-239, init_pcur :245-267, gen_proposal :361-411,
+//   calc_chi2_terms/calc_chi2 :273-350, spmp_mcmc :426-474,
+//   adjust_steps :480-526, replica_exchange :533-626, run_mcmc :682-763,
+// with the same per-replica order of random draws, so that with the same
+// seed it walks the same chains (cuRAND XORWOW, curand_init(seed, ist, 0)).
+#pragma once
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <curand_kernel.h>
+
+#include "cmc_job.h"
+
+namespace cmc {
+namespace cg = cooperative_groups;
+
+constexpr int kCH = 32;          // main iterations staged in smem per pout flush
+constexpr int kMaxThreads = 256;
+constexpr int kRepF = 4;         // per-replica floats: ptent, chi2c, chi2n, beta
+constexpr int kRepI = 4;         // per-replica ints: ptentn, flag, kchosen, evaluated
+constexpr int kMaxRetry = 64;    // bound on the k-redraw loops (u == 1.0 exactly)
+
+__device__ __forceinline__ void set_status(int *st, int code)
+{
+  if (st) atomicCAS(st, 0, code);
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One replica's random source: the reference's cuRAND XORWOW state, or an
+// injected stream pair with cursors.
+struct Rng {
+  curandStateXORWOW st;
+  const float *u, *n;
+  int cu, cn, lu, ln;
+  bool inj;
+  bool ovf;
+
+  __device__ float uniform()
+  {
+    if (inj) {
+      if (cu < lu) return u[cu++];
+      ovf = true;
+      return 0.5f;
+    }
+    return curand_uniform(&st);
+  }
+  __device__ float normal()
+  {
+    if (inj) {
+      if (cn < ln) return n[cn++];
+      ovf = true;
+      return 0.0f;
+    }
+    return curand_normal(&st);
+  }
+  // Index in [0, n) drawn as (int)(n*u), redrawn while it equals n
+  // (curand_uniform can return exactly 1.0), src/gpu_mcmc.cu:369-372.
+  __device__ int index(int n, int *status)
+  {
+    for (int t = 0; t < kMaxRetry; ++t) {
+      int k = (int)((float)n * uniform());
+      if (k < n) return k;
+    }
+    set_status(status, CMC_ERR_STREAM);
+    return n - 1;
+  }
+};
+
+__host__ __device__ inline unsigned align16(unsigned x) { return (x + 15u) & ~15u; }
+
+// Shared-memory plan of one CTA; the same function sizes the launch on the
+// host and carves the buffer on the device.
+struct SmemPlan {
+  unsigned params, plast, ptmp, rf, ri, sf, si, tab, consts, red, xch, stage,
+      scratch, total;
+};
+
+__host__ __device__ inline SmemPlan make_plan(int R, int nthreads, int nptot, int nprm,
+                                              int nbeta, unsigned consts_bytes,
+                                              unsigned scratch_bytes)
+{
+  SmemPlan p;
+  unsigned o = 0;
+  p.params = o;  o = align16(o + 4u * R * nptot);
+  p.plast = o;   o = align16(o + 4u * R * nptot);
+  p.ptmp = o;    o = align16(o + 4u * (R * nptot + R));
+  p.rf = o;      o = align16(o + 4u * R * kRepF);
+  p.ri = o;      o = align16(o + 4u * R * kRepI);
+  p.sf = o;      o = align16(o + 4u * R * nprm);
+  p.si = o;      o = align16(o + 4u * R * nprm * 3);
+  p.tab = o;     o = align16(o + 4u * (nprm + 3 * nptot));
+  p.consts = o;  o = align16(o + consts_bytes * R);
+  p.red = o;     o = align16(o + 4u * R * (nthreads / 32));
+  p.xch = o;     o = align16(o + 4u * 5 * nbeta);
+  p.stage = o;   o = align16(o + 4u * (R * nprm * kCH + nbeta * kCH + kCH));
+  p.scratch = o; o = align16(o + scratch_bytes);
+  p.total = o;
+  return p;
+}
+
+// Per-CTA view handed to the model policies.
+template <class Model, int R>
+struct Cta {
+  const cmc_job *job;
+  const typename Model::Packed *pk;
+  typename Model::Consts *consts;   // [R]
+  const int *flag;                  // [R]
+  float *scratch;
+  int ist[R];                       // global replica index of each local replica
+  int tid, nthreads;
+};
+
+template <class Model, int R>
+__device__ __forceinline__ void block_reduce(float (&acc)[R], float *red, int tid, int nw)
+{
+  const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    float v = warp_sum(acc[r]);
+    if (lane == 0) red[r * nw + warp] = v;
+  }
+}
+
+}  // namespace cmc

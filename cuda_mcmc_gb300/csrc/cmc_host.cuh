@@ -1,0 +1,522 @@
+// cmc_host.cuh -- host side of the C-ABI, shared by every model library.
+//
+// A model library is one translation unit that includes this header with
+// CMC_MODEL set to a model policy (SgraModel, PluginModel) and
+// CMC_MODEL_NAME to its name; it then exports the reference's entry points
+// (src/mcmc.h:7-32) plus the status-returning and device-pointer variants
+// declared in include/cuda_mcmc.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <type_traits>
+
+#include "cmc_common.cuh"
+#include "cmc_job.h"
+#include "cmc_launch.cuh"
+
+namespace cmc {
+
+inline std::string &last_error()
+{
+  static thread_local std::string e;
+  return e;
+}
+
+// Defined once per library (non-inline): the kernel-instance objects call it.
+int fail(int code, const std::string &msg)
+{
+  last_error() = msg;
+  return code;
+}
+
+inline int cuda_fail(cudaError_t e, const char *what)
+{
+  return fail(CMC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CMC_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+  } while (0)
+
+// Launch-shape override set by cmc_set_config (the autotuner) or the
+// CUDA_MCMC_R / CUDA_MCMC_THREADS environment variables; 0 = automatic.
+struct Override {
+  int R = 0, T = 0, phasor = -1;
+};
+inline Override &override_cfg()
+{
+  static Override o;
+  return o;
+}
+
+inline int env_int(const char *name, int dflt)
+{
+  const char *v = std::getenv(name);
+  return (v && *v) ? std::atoi(v) : dflt;
+}
+
+template <class F>
+inline int dispatch_R(int R, F &&f)
+{
+  switch (R) {
+    case 1: return f(std::integral_constant<int, 1>{});
+    case 2: return f(std::integral_constant<int, 2>{});
+    case 4: return f(std::integral_constant<int, 4>{});
+    case 8: return f(std::integral_constant<int, 8>{});
+    case 16: return f(std::integral_constant<int, 16>{});
+    case 32: return f(std::integral_constant<int, 32>{});
+    default: return fail(CMC_ERR_UNSUPPORTED, "no kernel instance for this replicas-per-CTA count");
+  }
+}
+
+inline int smem_optin()
+{
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v;
+}
+
+template <class Model>
+size_t plan_bytes(const cmc_job &j, const typename Model::Packed &pk, int R, int T, int sweep)
+{
+  if (sweep)
+    return make_plan(R, T, j.nptot, j.nprm, j.nbeta, sizeof(typename Model::Consts),
+                     Model::scratch_bytes(pk, R)).total;
+  return make_plan(R, T, j.nptot, 1, 1, sizeof(typename Model::Consts),
+                   Model::scratch_bytes(pk, R)).total;
+}
+
+// Pick replicas-per-CTA R (cluster size G = nbeta/R <= 16), threads T and the
+// phase storage mode.  Score = waves * R, proportional to the makespan when
+// every cluster carries the same work; ties go to the smaller R.
+template <class Model>
+int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &out)
+{
+  const Override &ov = override_cfg();
+  const int Rfix = ov.R ? ov.R : env_int("CUDA_MCMC_R", 0);
+  const int Tfix = ov.T ? ov.T : env_int("CUDA_MCMC_THREADS", 0);
+  const int Pfix = ov.phasor >= 0 ? ov.phasor : env_int("CUDA_MCMC_PHASOR", -1);
+  const int lim = smem_optin();
+  double best = 1e300;
+  bool found = false;
+  const int Rs[] = {1, 2, 4, 8, 16, 32};
+  for (int R : Rs) {
+    if (Rfix && R != Rfix) continue;
+    if (j.nbeta % R != 0) continue;
+    const int G = j.nbeta / R;
+    if (G > 16) continue;
+    const int Ts[] = {64, 128, 256};
+    for (int T : Ts) {
+      if (Tfix && T != Tfix) continue;
+      if (!Tfix && T == 64 && R > 4) continue;
+      for (int ph = 1; ph >= 0; --ph) {
+        if (Pfix >= 0 && ph != Pfix) continue;
+        typename Model::Packed q = pk;
+        q.phasor = ph;
+        const size_t smem = plan_bytes<Model>(j, q, R, T, 1);
+        if ((long long)smem > lim) continue;
+        const int n = dispatch_R(R, [&](auto rc) {
+          return sweep_capacity<Model, decltype(rc)::value>(G, T, smem, j.nseq);
+        });
+        if (n <= 0) continue;
+        const int waves = (j.nseq + n - 1) / n;
+        // prefer phasors (cheaper closures), then more threads per replica
+        const double score = (double)waves * R * (ph ? 1.0 : 1.15) * (T == 64 ? 1.1 : 1.0);
+        if (score < best - 1e-9) {
+          best = score;
+          out.R = R; out.G = G; out.T = T; out.phasor = ph; out.smem = smem;
+          out.clusters_per_wave = n;
+          found = true;
+        }
+        break;   // the phasor variant fitted: no need to try phases
+      }
+    }
+  }
+  if (!found)
+    return fail(CMC_ERR_UNSUPPORTED,
+                "no sweep launch shape fits: nbeta must be a multiple of a power of two "
+                "<= 32 with nbeta/R <= 16, and a CTA's replicas must fit in shared memory");
+  pk.phasor = out.phasor;
+  return CMC_OK;
+}
+
+inline int validate_common(const cmc_job &j, int mode)
+{
+  if (j.nbeta < 1 || j.nseq < 1 || j.nptot < 1 || j.ndat < 1)
+    return fail(CMC_ERR_ARG, "nbeta, nseq, nptot and ndat must be >= 1");
+  if ((long long)j.nbeta * j.nseq * (long long)std::max(j.ndat, j.nptot) > 0x7fffffffLL)
+    return fail(CMC_ERR_ARG, "nbeta*nseq*ndat exceeds the 32-bit index range");
+  if (!j.coor || !j.idat || !j.pcur || !j.status)
+    return fail(CMC_ERR_ARG, "coor, idat, pcur and status must be device pointers");
+  if (mode != 2 && (!j.dat || !j.std2r || !j.chi2c))
+    return fail(CMC_ERR_ARG, "dat, std2r and chi2c must be device pointers");
+  if (mode == 0) {
+    if (j.nbeta < 2)
+      return fail(CMC_ERR_ARG, "nbeta must be >= 2 (the replica exchange picks adjacent pairs)");
+    if (j.nprm < 1 || j.nprm > j.nptot)
+      return fail(CMC_ERR_ARG, "nprm must be in [1, nptot]");
+    if (j.nadj < 1) return fail(CMC_ERR_ARG, "nadj must be >= 1");
+    if (j.npass < 1) return fail(CMC_ERR_ARG, "npass must be >= 1");
+    if (j.nburn < 0 || j.niter < 0 || j.itr0 < 0 || j.itr0 + j.niter > j.niter_total)
+      return fail(CMC_ERR_ARG, "need nburn, niter >= 0 and itr0 + niter <= niter_total");
+    if (!j.pdescr || !j.ivar || !j.pmint || !j.pmaxt || !j.beta || !j.flag || !j.ptent ||
+        !j.ptentn || !j.pstp || !j.n_acpt || !j.n_exch || !j.n_cnt || !j.n_hist || !j.tcur)
+      return fail(CMC_ERR_ARG, "a sampler state array is missing");
+    if (j.niter > 0 && (!j.pout || !j.tout || !j.chi2))
+      return fail(CMC_ERR_ARG, "pout, tout and chi2 are required when niter > 0");
+    if (j.rng_mode == CMC_RNG_CURAND && !j.rndst)
+      return fail(CMC_ERR_ARG, "rndst is required for the cuRAND generator");
+    if (j.rng_mode == CMC_RNG_INJECTED && (!j.inj_u || !j.inj_n || !j.inj_cur))
+      return fail(CMC_ERR_ARG, "injected streams need inj_u, inj_n and inj_cur");
+  }
+  return CMC_OK;
+}
+
+template <class Model>
+int run_sweep(const cmc_job &j, cudaStream_t s, LaunchCfg *used = nullptr)
+{
+  int rc = validate_common(j, 0);
+  if (rc) return rc;
+  typename Model::Packed pk;
+  const char *err = nullptr;
+  rc = Model::host_dims(j, 0, pk, &err);
+  if (rc) return fail(rc, err);
+  if (Model::host_work_bytes(pk) > 0 && (j.work == nullptr || j.work_bytes < Model::host_work_bytes(pk)))
+    return fail(CMC_ERR_ARG, "job.work is smaller than cmc_work_bytes()");
+  LaunchCfg c;
+  rc = pick_sweep_config<Model>(j, pk, c);
+  if (rc) return rc;
+  rc = Model::host_pack(j, pk, j.work, s);
+  if (rc) return fail(rc, "packing the model data failed");
+  rc = dispatch_R(c.R, [&](auto rcnst) {
+    return launch_sweep<Model, decltype(rcnst)::value>(j, pk, c, s);
+  });
+  if (used) *used = c;
+  return rc;
+}
+
+template <class Model>
+int run_eval(const cmc_job &j, int mode, cudaStream_t s)
+{
+  int rc = validate_common(j, mode);
+  if (rc) return rc;
+  typename Model::Packed pk;
+  const char *err = nullptr;
+  rc = Model::host_dims(j, mode, pk, &err);
+  if (rc) return fail(rc, err);
+  if (Model::host_work_bytes(pk) > 0 && (j.work == nullptr || j.work_bytes < Model::host_work_bytes(pk)))
+    return fail(CMC_ERR_ARG, "job.work is smaller than cmc_work_bytes()");
+  pk.phasor = 0;
+  const int lim = smem_optin();
+  const int T = 128;
+  int R = 0;
+  size_t smem = 0;
+  const int Rs[] = {4, 2, 1};
+  for (int r : Rs) {
+    smem = plan_bytes<Model>(j, pk, r, T, 0);
+    if ((long long)smem <= lim) { R = r; break; }
+  }
+  if (!R) return fail(CMC_ERR_UNSUPPORTED, "one replica's model rows do not fit in shared memory");
+  rc = Model::host_pack(j, pk, j.work, s);
+  if (rc) return fail(rc, "packing the model data failed");
+  return dispatch_R(R, [&](auto rcnst) {
+    return launch_eval<Model, decltype(rcnst)::value>(j, pk, mode == 2 ? 1 : 0, T, smem, s);
+  });
+}
+
+template <class Model>
+size_t work_bytes(const cmc_job &j, int mode)
+{
+  typename Model::Packed pk;
+  const char *err = nullptr;
+  if (Model::host_dims(j, mode, pk, &err)) return 0;
+  return Model::host_work_bytes(pk);
+}
+
+// ---- the reference's host-pointer entry points ------------------------------
+
+// One device allocation carved into 256-byte aligned pieces.
+struct Arena {
+  size_t off = 0;
+  unsigned char *base = nullptr;
+  size_t take(size_t bytes)
+  {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  }
+  template <class T>
+  T *at(size_t o) const { return reinterpret_cast<T *>(base + o); }
+};
+
+template <class T>
+inline int h2d(T *dst, const T *src, size_t n, cudaStream_t s)
+{
+  if (n == 0 || src == nullptr) return CMC_OK;
+  CMC_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  return CMC_OK;
+}
+
+template <class T>
+inline int d2h(T *dst, const T *src, size_t n, cudaStream_t s)
+{
+  if (n == 0 || dst == nullptr) return CMC_OK;
+  CMC_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+  return CMC_OK;
+}
+
+struct DevBuf {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  ~DevBuf()
+  {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+inline int read_status(const int *dstatus, cudaStream_t s, int *out)
+{
+  CMC_CUDA(cudaMemcpyAsync(out, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CMC_CUDA(cudaStreamSynchronize(s));
+  return CMC_OK;
+}
+
+inline const char *status_text(int st)
+{
+  switch (st) {
+    case CMC_ERR_ARG: return "invalid input detected on the device (e.g. a closure index out of range)";
+    case CMC_ERR_STREAM: return "an injected random stream ran out";
+    case CMC_ERR_MODEL: return "the model reported an error";
+    default: return "device error";
+  }
+}
+
+template <class Model>
+int host_mcmc(float *coor, float *dat, float *std2r, int *icoor, int *idat, float *datm,
+              float *chi2m, int *pdescr, int *ivar, int *invar, float *ptotal, float *pmint,
+              float *pmaxt, float *pout, int *tout, float *chi2, float *chi2c, int *tcur,
+              int *flag, int *n_acpt, int *n_exch, int *n_cnt, int *n_hist, float *beta,
+              float *pstp, float *ptent, int *ptentn, float *pcur, unsigned char *rndst,
+              unsigned long long seed, int imodel, int ncoor, int ndat, int nicoor, int nidat,
+              int ndatm, int nptot, int nprm, int nadj, int npass, int nbeta, int nseq,
+              int nburn, int niter)
+{
+  (void)ptotal;
+  if (!coor || !dat || !std2r || !idat || !datm || !chi2m || !pdescr || !ivar || !invar ||
+      !pmint || !pmaxt || !chi2c || !tcur || !flag || !n_acpt || !n_exch || !n_cnt ||
+      !n_hist || !beta || !pstp || !ptent || !ptentn || !pcur || !rndst)
+    return fail(CMC_ERR_ARG, "mcmc_cuda: a required array pointer is NULL");
+  if (niter > 0 && (!pout || !tout || !chi2))
+    return fail(CMC_ERR_ARG, "mcmc_cuda: pout, tout and chi2 are required when niter > 0");
+  if (nptot < 1 || nprm < 1 || nprm > nptot || nbeta < 2 || nseq < 1 || ndat < 1 ||
+      nadj < 1 || npass < 1 || nburn < 0 || niter < 0 || nidat < 1 || ncoor < 0 || nicoor < 0)
+    return fail(CMC_ERR_ARG, "mcmc_cuda: invalid sizes");
+  for (int k = 0; k < nprm; ++k) {
+    if (ivar[k] < 0 || ivar[k] >= nptot || invar[ivar[k]] != k)
+      return fail(CMC_ERR_ARG, "mcmc_cuda: ivar/invar are not inverse maps of the mutable "
+                               "parameters (ivar[k] in [0,nptot), invar[ivar[k]] == k)");
+  }
+  const size_t nrep = (size_t)nbeta * nseq;
+  cudaStream_t s = cudaStreamPerThread;
+
+  cmc_job j;
+  std::memset(&j, 0, sizeof(j));
+  j.ncoor = ncoor; j.ndat = ndat; j.nicoor = nicoor; j.nidat = nidat; j.ndatm = ndatm;
+  j.nptot = nptot; j.nprm = nprm; j.nadj = nadj; j.npass = npass; j.nbeta = nbeta;
+  j.nseq = nseq; j.imodel = imodel;
+  j.do_init = 1; j.nburn = nburn; j.niter = niter; j.itr0 = 0; j.niter_total = niter;
+  j.rng_mode = CMC_RNG_CURAND; j.seed = seed;
+  for (int i = 0; i < 4; ++i) j.hidat[i] = i < nidat ? idat[i] : 0;
+
+  Arena a;
+  const size_t o_coor = a.take(4 * (size_t)ncoor), o_dat = a.take(4 * (size_t)ndat),
+               o_std = a.take(4 * (size_t)ndat), o_icoor = a.take(4 * (size_t)std::max(nicoor, 1)),
+               o_idat = a.take(4 * (size_t)nidat), o_datm = a.take(4 * (size_t)ndatm),
+               o_chi2m = a.take(4 * nrep * ndat), o_pdescr = a.take(4 * (size_t)nptot),
+               o_ivar = a.take(4 * (size_t)nprm), o_invar = a.take(4 * (size_t)nptot),
+               o_pmin = a.take(4 * (size_t)nptot), o_pmax = a.take(4 * (size_t)nptot),
+               o_pout = a.take(4 * (size_t)nprm * nrep * niter), o_tout = a.take(4 * nrep * niter),
+               o_chi2 = a.take(4 * (size_t)nseq * niter), o_chi2c = a.take(4 * nrep),
+               o_tcur = a.take(4 * nrep), o_flag = a.take(4 * nrep),
+               o_nacpt = a.take(4 * nprm * nrep), o_nexch = a.take(4 * nrep),
+               o_ncnt = a.take(4 * nprm * nrep), o_nhist = a.take(4 * (size_t)nadj * nprm * nrep),
+               o_beta = a.take(4 * (size_t)nbeta), o_pstp = a.take(4 * nprm * nrep),
+               o_ptent = a.take(4 * nrep), o_ptentn = a.take(4 * nrep),
+               o_pcur = a.take(4 * nrep * nptot), o_rndst = a.take(48 * nrep),
+               o_status = a.take(16);
+  // model scratch, sized with the final device pointers unknown yet: dims only
+  {
+    cmc_job probe = j;
+    probe.datm = reinterpret_cast<float *>(16);
+    probe.chi2m = reinterpret_cast<float *>(16);
+    j.work_bytes = work_bytes<Model>(probe, 0);
+  }
+  const size_t o_work = a.take(j.work_bytes);
+
+  DevBuf buf;
+  buf.s = s;
+  {
+    cudaError_t e = cudaMallocAsync(&buf.p, a.off, s);
+    if (e != cudaSuccess) {
+      buf.p = nullptr;
+      return fail(CMC_ERR_NOMEM, std::string("mcmc_cuda: device allocation failed: ") +
+                                     cudaGetErrorString(e));
+    }
+  }
+  a.base = (unsigned char *)buf.p;
+  j.coor = a.at<float>(o_coor); j.dat = a.at<float>(o_dat); j.std2r = a.at<float>(o_std);
+  j.icoor = a.at<int>(o_icoor); j.idat = a.at<int>(o_idat);
+  j.datm = a.at<float>(o_datm); j.chi2m = a.at<float>(o_chi2m);
+  j.pdescr = a.at<int>(o_pdescr); j.ivar = a.at<int>(o_ivar); j.invar = a.at<int>(o_invar);
+  j.pmint = a.at<float>(o_pmin); j.pmaxt = a.at<float>(o_pmax);
+  j.pout = a.at<float>(o_pout); j.tout = a.at<int>(o_tout); j.chi2 = a.at<float>(o_chi2);
+  j.chi2c = a.at<float>(o_chi2c); j.tcur = a.at<int>(o_tcur); j.flag = a.at<int>(o_flag);
+  j.n_acpt = a.at<int>(o_nacpt); j.n_exch = a.at<int>(o_nexch); j.n_cnt = a.at<int>(o_ncnt);
+  j.n_hist = a.at<int>(o_nhist); j.beta = a.at<float>(o_beta); j.pstp = a.at<float>(o_pstp);
+  j.ptent = a.at<float>(o_ptent); j.ptentn = a.at<int>(o_ptentn); j.pcur = a.at<float>(o_pcur);
+  j.rndst = a.at<unsigned char>(o_rndst); j.status = a.at<int>(o_status);
+  j.work = j.work_bytes ? (void *)a.at<unsigned char>(o_work) : nullptr;
+
+  int rc = CMC_OK;
+#define CMC_TRY(x) do { if ((rc = (x)) != CMC_OK) return rc; } while (0)
+  CMC_TRY(h2d(const_cast<float *>(j.coor), coor, ncoor, s));
+  CMC_TRY(h2d(const_cast<float *>(j.dat), dat, ndat, s));
+  CMC_TRY(h2d(const_cast<float *>(j.std2r), std2r, ndat, s));
+  CMC_TRY(h2d(const_cast<int *>(j.icoor), icoor, nicoor, s));
+  CMC_TRY(h2d(const_cast<int *>(j.idat), idat, nidat, s));
+  if (Model::kRowsInEval) {   // a plugin's chi^2 sums whole chi2m rows
+    CMC_TRY(h2d(j.datm, datm, ndatm, s));
+    CMC_TRY(h2d(j.chi2m, chi2m, nrep * ndat, s));
+  }
+  CMC_TRY(h2d(const_cast<int *>(j.pdescr), pdescr, nptot, s));
+  CMC_TRY(h2d(const_cast<int *>(j.ivar), ivar, nprm, s));
+  CMC_TRY(h2d(const_cast<int *>(j.invar), invar, nptot, s));
+  CMC_TRY(h2d(const_cast<float *>(j.pmint), pmint, nptot, s));
+  CMC_TRY(h2d(const_cast<float *>(j.pmaxt), pmaxt, nptot, s));
+  CMC_TRY(h2d(j.tcur, tcur, nrep, s));
+  CMC_TRY(h2d(j.flag, flag, nrep, s));
+  CMC_TRY(h2d(j.chi2c, chi2c, nrep, s));
+  CMC_TRY(h2d(j.n_acpt, n_acpt, nprm * nrep, s));
+  CMC_TRY(h2d(j.n_exch, n_exch, nrep, s));
+  CMC_TRY(h2d(j.n_cnt, n_cnt, nprm * nrep, s));
+  CMC_TRY(h2d(j.n_hist, n_hist, (size_t)nadj * nprm * nrep, s));
+  CMC_TRY(h2d(const_cast<float *>(j.beta), beta, nbeta, s));
+  CMC_TRY(h2d(j.pstp, pstp, nprm * nrep, s));
+  CMC_TRY(h2d(j.ptent, ptent, nrep, s));
+  CMC_TRY(h2d(j.ptentn, ptentn, nrep, s));
+  CMC_TRY(h2d(j.pcur, pcur, nrep * nptot, s));
+  CMC_CUDA(cudaMemsetAsync(j.status, 0, sizeof(int), s));
+
+  CMC_TRY(run_sweep<Model>(j, s));
+
+  CMC_TRY(d2h(rndst, j.rndst, 48 * nrep, s));
+  CMC_TRY(d2h(pout, j.pout, (size_t)nprm * nrep * niter, s));
+  CMC_TRY(d2h(tout, j.tout, nrep * niter, s));
+  CMC_TRY(d2h(chi2, j.chi2, (size_t)nseq * niter, s));
+  CMC_TRY(d2h(tcur, j.tcur, nrep, s));
+  CMC_TRY(d2h(n_acpt, j.n_acpt, nprm * nrep, s));
+  CMC_TRY(d2h(n_cnt, j.n_cnt, nprm * nrep, s));
+  CMC_TRY(d2h(n_exch, j.n_exch, nrep, s));
+  CMC_TRY(d2h(n_hist, j.n_hist, (size_t)nadj * nprm * nrep, s));
+  CMC_TRY(d2h(pstp, j.pstp, nprm * nrep, s));
+  CMC_TRY(d2h(ptent, j.ptent, nrep, s));
+  CMC_TRY(d2h(ptentn, j.ptentn, nrep, s));
+  CMC_TRY(d2h(pcur, j.pcur, nrep * nptot, s));
+  CMC_TRY(d2h(flag, j.flag, nrep, s));
+  CMC_TRY(d2h(chi2c, j.chi2c, nrep, s));
+  CMC_TRY(d2h(datm, j.datm, (size_t)ndatm, s));
+  CMC_TRY(d2h(chi2m, j.chi2m, nrep * ndat, s));
+  int st = 0;
+  CMC_TRY(read_status(j.status, s, &st));
+#undef CMC_TRY
+  if (st) return fail(st, std::string("mcmc_cuda: ") + status_text(st));
+  return CMC_OK;
+}
+
+template <class Model>
+int host_eval(int mode, float *coor, float *dat, float *std2r, int *icoor, int *idat,
+              float *datm, float *chi2m, float *pcur, float *chi2c, int *flag, int imodel,
+              int ncoor, int ndat, int nicoor, int nidat, int ndatm, int nptot, int nbeta,
+              int nseq)
+{
+  if (!coor || !idat || !datm || !pcur || (mode == 1 && (!dat || !std2r || !chi2m || !chi2c)))
+    return fail(CMC_ERR_ARG, "a required array pointer is NULL");
+  if (nptot < 1 || nbeta < 1 || nseq < 1 || ndat < 1 || nidat < 1 || ncoor < 0 || nicoor < 0 ||
+      ndatm < 0)
+    return fail(CMC_ERR_ARG, "invalid sizes");
+  const size_t nrep = (size_t)nbeta * nseq;
+  cudaStream_t s = cudaStreamPerThread;
+  cmc_job j;
+  std::memset(&j, 0, sizeof(j));
+  j.ncoor = ncoor; j.ndat = ndat; j.nicoor = nicoor; j.nidat = nidat; j.ndatm = ndatm;
+  j.nptot = nptot; j.nbeta = nbeta; j.nseq = nseq; j.imodel = imodel; j.npass = 2;
+  for (int i = 0; i < 4; ++i) j.hidat[i] = i < nidat ? idat[i] : 0;
+  Arena a;
+  const size_t o_coor = a.take(4 * (size_t)ncoor), o_dat = a.take(4 * (size_t)ndat),
+               o_std = a.take(4 * (size_t)ndat), o_icoor = a.take(4 * (size_t)std::max(nicoor, 1)),
+               o_idat = a.take(4 * (size_t)nidat), o_datm = a.take(4 * (size_t)std::max(ndatm, 1)),
+               o_chi2m = a.take(4 * nrep * ndat), o_pcur = a.take(4 * nrep * nptot),
+               o_chi2c = a.take(4 * nrep), o_flag = a.take(4 * nrep), o_status = a.take(16);
+  {
+    cmc_job probe = j;
+    probe.datm = reinterpret_cast<float *>(16);
+    probe.chi2m = reinterpret_cast<float *>(16);
+    j.work_bytes = work_bytes<Model>(probe, mode);
+  }
+  const size_t o_work = a.take(j.work_bytes);
+  DevBuf buf;
+  buf.s = s;
+  if (cudaMallocAsync(&buf.p, a.off, s) != cudaSuccess) {
+    buf.p = nullptr;
+    return fail(CMC_ERR_NOMEM, "device allocation failed");
+  }
+  a.base = (unsigned char *)buf.p;
+  j.coor = a.at<float>(o_coor); j.dat = a.at<float>(o_dat); j.std2r = a.at<float>(o_std);
+  j.icoor = a.at<int>(o_icoor); j.idat = a.at<int>(o_idat); j.datm = a.at<float>(o_datm);
+  j.chi2m = a.at<float>(o_chi2m); j.pcur = a.at<float>(o_pcur); j.chi2c = a.at<float>(o_chi2c);
+  j.flag = a.at<int>(o_flag); j.status = a.at<int>(o_status);
+  j.work = j.work_bytes ? (void *)a.at<unsigned char>(o_work) : nullptr;
+  int rc = CMC_OK;
+#define CMC_TRY(x) do { if ((rc = (x)) != CMC_OK) return rc; } while (0)
+  CMC_TRY(h2d(const_cast<float *>(j.coor), coor, ncoor, s));
+  CMC_TRY(h2d(const_cast<int *>(j.idat), idat, nidat, s));
+  CMC_TRY(h2d(j.pcur, pcur, nrep * nptot, s));
+  CMC_TRY(h2d(j.datm, datm, (size_t)ndatm, s));
+  if (mode == 1) {
+    CMC_TRY(h2d(const_cast<float *>(j.dat), dat, ndat, s));
+    CMC_TRY(h2d(const_cast<float *>(j.std2r), std2r, ndat, s));
+    CMC_TRY(h2d(const_cast<int *>(j.icoor), icoor, nicoor, s));
+    CMC_TRY(h2d(j.chi2m, chi2m, nrep * ndat, s));
+    CMC_TRY(h2d(j.chi2c, chi2c, nrep, s));
+  }
+  if (flag && mode == 1) {
+    CMC_TRY(h2d(j.flag, flag, nrep, s));
+  } else {
+    // calc_model: the reference leaves flag uninitialised (src/mcmcjob.cu:269);
+    // every parameter set is evaluated here.
+    CMC_CUDA(cudaMemsetAsync(j.flag, 0, 4 * nrep, s));
+    j.flag = nullptr;
+  }
+  CMC_CUDA(cudaMemsetAsync(j.status, 0, sizeof(int), s));
+  CMC_TRY(run_eval<Model>(j, mode, s));
+  CMC_TRY(d2h(datm, j.datm, (size_t)ndatm, s));
+  if (mode == 1) {
+    CMC_TRY(d2h(chi2m, j.chi2m, nrep * ndat, s));
+    CMC_TRY(d2h(chi2c, j.chi2c, nrep, s));
+  }
+  int st = 0;
+  CMC_TRY(read_status(j.status, s, &st));
+#undef CMC_TRY
+  if (st) return fail(st, status_text(st));
+  return CMC_OK;
+}
+
+}  // namespace cmc

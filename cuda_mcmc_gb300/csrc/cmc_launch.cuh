@@ -1,0 +1,33 @@
+// cmc_launch.cuh -- launch entry points of the kernel instances.
+//
+// Each (model, R) kernel instance is compiled in its own translation unit
+// (inst_*.cu with -DCMC_R=R, see cmc_launch_impl.cuh) so that a library builds
+// in parallel; the host layer only sees these declarations.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "cmc_job.h"
+
+namespace cmc {
+
+struct LaunchCfg {
+  int R = 0, G = 0, T = 0, phasor = 1, clusters_per_wave = 0;
+  size_t smem = 0;
+};
+
+// Clusters of G CTAs (T threads, smem bytes) that can be resident at once;
+// 0 when the configuration does not fit.
+template <class Model, int R>
+int sweep_capacity(int G, int T, size_t smem, int nseq);
+
+template <class Model, int R>
+int launch_sweep(const cmc_job &j, const typename Model::Packed &pk, const LaunchCfg &c,
+                 cudaStream_t s);
+
+template <class Model, int R>
+int launch_eval(const cmc_job &j, const typename Model::Packed &pk, int model_only, int T,
+                size_t smem, cudaStream_t s);
+
+}  // namespace cmc

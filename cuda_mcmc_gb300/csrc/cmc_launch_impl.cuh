@@ -1,0 +1,99 @@
+// cmc_launch_impl.cuh -- definitions behind cmc_launch.cuh.  Included by the
+// instance translation units only (inst_sgra.cu, inst_plugin.cu), each of
+// which instantiates one value of R for its model.
+#pragma once
+#include <string>
+
+#include "cmc_eval.cuh"
+#include "cmc_launch.cuh"
+#include "cmc_sweep.cuh"
+
+namespace cmc {
+
+int fail(int code, const std::string &msg);   // cmc_host.cuh (library TU)
+
+template <class Model, int R>
+int sweep_capacity(int G, int T, size_t smem, int nseq)
+{
+  auto kern = sweep_kernel<Model, R>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (G > 8 &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(G * nseq);
+  cfg.blockDim = dim3(T);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, (void *)kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+template <class Model, int R>
+int launch_sweep(const cmc_job &j, const typename Model::Packed &pk, const LaunchCfg &c,
+                 cudaStream_t s)
+{
+  auto kern = sweep_kernel<Model, R>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+  if (e == cudaSuccess && c.G > 8)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("sweep kernel attributes: ") + cudaGetErrorString(e));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = c.G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(c.G * j.nseq);
+  cfg.blockDim = dim3(c.T);
+  cfg.dynamicSmemBytes = c.smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, j, pk);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("sweep kernel launch: ") + cudaGetErrorString(e));
+  return CMC_OK;
+}
+
+template <class Model, int R>
+int launch_eval(const cmc_job &j, const typename Model::Packed &pk, int model_only, int T,
+                size_t smem, cudaStream_t s)
+{
+  auto kern = eval_kernel<Model, R>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("eval kernel attributes: ") + cudaGetErrorString(e));
+  const int nrep = j.nbeta * j.nseq;
+  kern<<<(nrep + R - 1) / R, T, smem, s>>>(j, pk, model_only);
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("eval kernel launch: ") + cudaGetErrorString(e));
+  return CMC_OK;
+}
+
+#define CMC_INSTANTIATE(MODEL, RV)                                                        \
+  template int sweep_capacity<MODEL, RV>(int, int, size_t, int);                          \
+  template int launch_sweep<MODEL, RV>(const cmc_job &, const MODEL::Packed &,           \
+                                       const LaunchCfg &, cudaStream_t);                  \
+  template int launch_eval<MODEL, RV>(const cmc_job &, const MODEL::Packed &, int, int,  \
+                                      size_t, cudaStream_t);
+
+}  // namespace cmc

@@ -1,0 +1,339 @@
+// cmc_sweep.cuh -- the fused MCMC-RE sweep kernel (one launch per run).
+// The work decomposition and the reference functions it restates are
+// described at the top of cmc_common.cuh.
+#pragma once
+#include "cmc_common.cuh"
+
+namespace cmc {
+
+template <class Model, int R>
+__global__ void __launch_bounds__(kMaxThreads)
+sweep_kernel(const cmc_job job, const typename Model::Packed pk)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int G = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int iseq = blockIdx.x / G;
+  const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
+  const int nbeta = job.nbeta, nseq = job.nseq, nptot = job.nptot, nprm = job.nprm;
+  const int nadj = job.nadj;
+
+  const SmemPlan P = make_plan(R, T, nptot, nprm, nbeta, sizeof(typename Model::Consts),
+                               Model::scratch_bytes(pk, R));
+  float *params = (float *)(smem + P.params);   // [R][nptot]
+  float *plast = (float *)(smem + P.plast);     // [R][nptot] params of last evaluation
+  float *ptmp = (float *)(smem + P.ptmp);       // [R][nptot] + [R] exchange staging
+  float *rf = (float *)(smem + P.rf);
+  int *ri = (int *)(smem + P.ri);
+  float *s_ptent = rf, *s_chi2c = rf + R, *s_chi2n = rf + 2 * R, *s_beta = rf + 3 * R;
+  int *s_ptentn = ri, *s_flag = ri + R, *s_k = ri + 2 * R, *s_evald = ri + 3 * R;
+  float *s_pstp = (float *)(smem + P.sf);       // [R][nprm]
+  int *s_ncnt = (int *)(smem + P.si);           // [R][nprm]
+  int *s_nacpt = s_ncnt + R * nprm;
+  int *s_hsum = s_nacpt + R * nprm;
+  int *s_ivar = (int *)(smem + P.tab);
+  int *s_pdescr = s_ivar + nprm;
+  float *s_pmin = (float *)(s_pdescr + nptot);
+  float *s_pmax = s_pmin + nptot;
+  typename Model::Consts *s_consts = (typename Model::Consts *)(smem + P.consts);
+  float *s_red = (float *)(smem + P.red);       // [R][NW]
+  float *x_chi2 = (float *)(smem + P.xch);      // rank 0: [nbeta] each
+  int *x_perm = (int *)(x_chi2 + nbeta);
+  int *x_tcur = x_perm + nbeta;
+  int *x_nexch = x_tcur + nbeta;
+  float *x_beta = (float *)(x_nexch + nbeta);
+  float *st_p = (float *)(smem + P.stage);      // [R][nprm][kCH]
+  int *st_t = (int *)(st_p + R * nprm * kCH);   // [nbeta][kCH] (rank 0)
+  float *st_c = (float *)(st_t + nbeta * kCH);  // [kCH] (rank 0)
+  float *scratch = (float *)(smem + P.scratch);
+
+  Cta<Model, R> cta;
+  cta.job = &job;
+  cta.pk = &pk;
+  cta.consts = s_consts;
+  cta.flag = s_flag;
+  cta.scratch = scratch;
+  cta.tid = tid;
+  cta.nthreads = T;
+#pragma unroll
+  for (int r = 0; r < R; ++r) cta.ist[r] = (rank * R + r) * nseq + iseq;
+
+  // ---- load tables and state -------------------------------------------
+  for (int i = tid; i < nprm; i += T) s_ivar[i] = job.ivar[i];
+  for (int i = tid; i < nptot; i += T) {
+    s_pdescr[i] = job.pdescr[i];
+    s_pmin[i] = job.pmint[i];
+    s_pmax[i] = job.pmaxt[i];
+  }
+  for (int i = tid; i < R * nptot; i += T) {
+    int r = i / nptot, j = i - r * nptot;
+    int ist = (rank * R + r) * nseq + iseq;
+    params[i] = job.pcur[(size_t)ist * nptot + j];
+    plast[i] = params[i];
+  }
+  for (int i = tid; i < R * nprm; i += T) {
+    int r = i / nprm, k = i - r * nprm, ibeta = rank * R + r;
+    size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
+    s_pstp[i] = job.pstp[gi];
+    s_ncnt[i] = job.n_cnt[gi];
+    s_nacpt[i] = job.n_acpt[gi];
+    int h = 0;
+    for (int a = 0; a < nadj; ++a)
+      h += job.n_hist[(((size_t)nprm * a + k) * nbeta + ibeta) * nseq + iseq];
+    s_hsum[i] = h;
+  }
+  if (rank == 0) {
+    for (int s = tid; s < nbeta; s += T) {
+      x_tcur[s] = job.tcur[s * nseq + iseq];
+      x_nexch[s] = job.n_exch[s * nseq + iseq];
+      x_beta[s] = job.beta[s];
+    }
+  }
+
+  Rng rng;
+  rng.inj = (job.rng_mode == CMC_RNG_INJECTED);
+  rng.ovf = false;
+  rng.u = rng.n = nullptr;
+  rng.cu = rng.cn = rng.lu = rng.ln = 0;
+  if (tid < R) {
+    const int r = tid, ibeta = rank * R + r, ist = ibeta * nseq + iseq;
+    s_ptent[r] = job.ptent[ist];
+    s_chi2c[r] = job.chi2c[ist];
+    s_beta[r] = job.beta[ibeta];
+    s_ptentn[r] = job.ptentn[ist];
+    s_flag[r] = job.flag[ist];
+    s_k[r] = 0;
+    s_evald[r] = 0;
+    if (rng.inj) {
+      rng.u = job.inj_u + (size_t)ist * job.inj_lu;
+      rng.n = job.inj_n + (size_t)ist * job.inj_ln;
+      rng.lu = job.inj_lu;
+      rng.ln = job.inj_ln;
+      rng.cu = job.do_init ? 0 : job.inj_cur[2 * ist];
+      rng.cn = job.do_init ? 0 : job.inj_cur[2 * ist + 1];
+    } else if (job.do_init) {
+      curand_init(job.seed, (unsigned long long)ist, 0ull, &rng.st);
+    } else {
+      rng.st = reinterpret_cast<const curandStateXORWOW *>(job.rndst)[ist];
+    }
+  }
+  Model::setup(cta, tid, T);
+  __syncthreads();
+
+  // ---- init_pcur + first chi^2 (src/gpu_mcmc.cu:245-267, 714-719) ---------
+  if (job.do_init) {
+    if (tid < R) {
+      const int r = tid;
+      s_flag[r] = 1;
+      for (int i = 0; i < nprm; ++i) {
+        int k = s_ivar[i];
+        float u = rng.uniform();
+        float p = __fmaf_rn(s_pmax[k] - s_pmin[k], u, s_pmin[k]);
+        if (s_pdescr[k] == 2) p = atan2f(sinf(p), cosf(p));
+        params[r * nptot + k] = p;
+      }
+      for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
+      Model::prepare(cta, r, &params[r * nptot]);
+      s_evald[r] = 1;
+    }
+    __syncthreads();
+    float acc[R];
+    Model::template eval<R>(cta, acc);
+    block_reduce<Model, R>(acc, s_red, tid, NW);
+    __syncthreads();
+    if (tid < R) {
+      float s = 0.f;
+      for (int w = 0; w < NW; ++w) s += s_red[tid * NW + w];
+      s_chi2c[tid] = s;
+    }
+    __syncthreads();
+  }
+
+  const int nsteps = job.nburn + job.niter;
+  for (int step = 0; step < nsteps; ++step) {
+    const bool burn = step < job.nburn;
+    for (int ipm = 0; ipm < nprm; ++ipm) {
+      // gen_proposal (src/gpu_mcmc.cu:361-411)
+      if (tid < R) {
+        const int r = tid;
+        const int k = rng.index(nprm, job.status);
+        const int t = s_ivar[k];
+        float p = params[r * nptot + t];
+        s_k[r] = k;
+        s_ptentn[r] = t;
+        s_ptent[r] = p;
+        const float sd = s_pstp[r * nprm + k];
+        const float rn = rng.normal();
+        p = __fmaf_rn(sd, rn, p);
+        if (s_pdescr[t] == 2) p = atan2f(sinf(p), cosf(p));
+        if ((p < s_pmin[t]) || (p > s_pmax[t])) {
+          s_flag[r] = 0;
+        } else {
+          s_flag[r] = 1;
+          params[r * nptot + t] = p;
+          for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
+          Model::prepare(cta, r, &params[r * nptot]);
+          s_evald[r] = 1;
+        }
+      }
+      __syncthreads();
+      // calc_chi2_terms x npass + the chi^2 sum (src/gpu_mcmc.cu:273-325, 447-448)
+      float acc[R];
+      Model::template eval<R>(cta, acc);
+      block_reduce<Model, R>(acc, s_red, tid, NW);
+      __syncthreads();
+      // spmp_mcmc (src/gpu_mcmc.cu:426-474) and adjust_steps (:480-526)
+      if (tid < R) {
+        const int r = tid, ibeta = rank * R + r;
+        const int k = s_k[r];
+        if (s_flag[r] != 0) {
+          float c2 = 0.f;
+          for (int w = 0; w < NW; ++w) c2 += s_red[r * NW + w];
+          s_chi2n[r] = c2;
+          const float a = expf(-0.5f * s_beta[r] * (c2 - s_chi2c[r]));
+          const float alpha = (a < 1.0f) ? a : 1.0f;
+          const float u = rng.uniform();
+          if (u <= alpha) {
+            s_chi2c[r] = c2;
+            s_nacpt[r * nprm + k] += 1;
+          } else {
+            params[r * nptot + s_ptentn[r]] = s_ptent[r];
+            s_flag[r] = 0;
+          }
+        }
+        if (burn) {
+          const int ik = r * nprm + k;
+          const int cnt = s_ncnt[ik];
+          int modn = cnt % nadj;
+          if (modn < 0) modn += nadj;   // guards a negative n_cnt from the caller
+          int *hp = &job.n_hist[(((size_t)nprm * modn + k) * nbeta + ibeta) * nseq + iseq];
+          const int nw = (s_flag[r] != 0) ? 1 : 0;
+          s_hsum[ik] += nw - *hp;
+          *hp = nw;
+          const float rate = (float)s_hsum[ik] / (float)((nadj < cnt) ? nadj : cnt);
+          if (rate < 0.30f)
+            s_pstp[ik] = (float)((double)s_pstp[ik] / 1.01);
+          else
+            s_pstp[ik] = (float)((double)s_pstp[ik] * 1.01);
+          s_ncnt[ik] = cnt + 1;
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- replica_exchange (src/gpu_mcmc.cu:533-626) ------------------------
+    cluster.sync();
+    if (rank == 0 && tid == 0) {
+      for (int s = 0; s < nbeta; ++s) {
+        const float *rc = cluster.map_shared_rank(s_chi2c, s / R);
+        x_chi2[s] = rc[s % R];
+        x_perm[s] = s;
+      }
+      const int nb1 = nbeta - 1;
+      for (int ib = 0; ib < nbeta; ++ib) {
+        const int k = rng.index(nb1, job.status);
+        const float a = expf(-0.5f * (x_beta[k + 1] - x_beta[k]) * (x_chi2[k] - x_chi2[k + 1]));
+        const float alpha = (a < 1.0f) ? a : 1.0f;
+        const float u = rng.uniform();
+        if (u <= alpha) {
+          int ti = x_tcur[k]; x_tcur[k] = x_tcur[k + 1]; x_tcur[k + 1] = ti;
+          int pi = x_perm[k]; x_perm[k] = x_perm[k + 1]; x_perm[k + 1] = pi;
+          float cc = x_chi2[k]; x_chi2[k] = x_chi2[k + 1]; x_chi2[k + 1] = cc;
+          if (!burn) x_nexch[k] += 1;
+        }
+      }
+    }
+    cluster.sync();
+    {
+      const int *perm0 = cluster.map_shared_rank(x_perm, 0);
+      const float *chi0 = cluster.map_shared_rank(x_chi2, 0);
+      for (int i = tid; i < R * nptot; i += T) {
+        int r = i / nptot, j = i - r * nptot;
+        int src = perm0[rank * R + r];
+        const float *rp = cluster.map_shared_rank(params, src / R);
+        ptmp[i] = rp[(src % R) * nptot + j];
+      }
+      if (tid < R) ptmp[R * nptot + tid] = chi0[rank * R + tid];
+    }
+    cluster.sync();
+    for (int i = tid; i < R * nptot; i += T) params[i] = ptmp[i];
+    if (tid < R) s_chi2c[tid] = ptmp[R * nptot + tid];
+    __syncthreads();
+    Model::after_exchange(cta);
+
+    // ---- record pout / tout / chi2 (main stage) ---------------------------
+    if (!burn) {
+      const int m = step - job.nburn;
+      const int slot = m % kCH;
+      for (int i = tid; i < R * nprm; i += T) {
+        int r = i / nprm, k = i - r * nprm;
+        st_p[i * kCH + slot] = params[r * nptot + s_ivar[k]];
+      }
+      if (rank == 0) {
+        for (int s = tid; s < nbeta; s += T) st_t[s * kCH + slot] = x_tcur[s];
+        if (tid == 0) st_c[slot] = x_chi2[0];
+      }
+      if (slot == kCH - 1 || m == job.niter - 1) {
+        __syncthreads();
+        const int cnt = slot + 1;
+        const size_t col0 = (size_t)job.itr0 + (m - slot);
+        const size_t ntot = (size_t)job.niter_total;
+        for (int i = tid; i < R * nprm * cnt; i += T) {
+          int rk = i / cnt, c = i - rk * cnt;
+          int r = rk / nprm, k = rk - r * nprm, ibeta = rank * R + r;
+          job.pout[(((size_t)k * nbeta + ibeta) * nseq + iseq) * ntot + col0 + c] =
+              st_p[rk * kCH + c];
+        }
+        if (rank == 0) {
+          for (int i = tid; i < nbeta * cnt; i += T) {
+            int s = i / cnt, c = i - s * cnt;
+            job.tout[((size_t)s * nseq + iseq) * ntot + col0 + c] = st_t[s * kCH + c];
+          }
+          for (int c = tid; c < cnt; c += T) job.chi2[(size_t)iseq * ntot + col0 + c] = st_c[c];
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // ---- write the state back ------------------------------------------------
+  for (int i = tid; i < R * nptot; i += T) {
+    int r = i / nptot, j = i - r * nptot;
+    int ist = (rank * R + r) * nseq + iseq;
+    job.pcur[(size_t)ist * nptot + j] = params[i];
+  }
+  for (int i = tid; i < R * nprm; i += T) {
+    int r = i / nprm, k = i - r * nprm, ibeta = rank * R + r;
+    size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
+    job.pstp[gi] = s_pstp[i];
+    job.n_cnt[gi] = s_ncnt[i];
+    job.n_acpt[gi] = s_nacpt[i];
+  }
+  if (rank == 0) {
+    for (int s = tid; s < nbeta; s += T) {
+      job.tcur[s * nseq + iseq] = x_tcur[s];
+      job.n_exch[s * nseq + iseq] = x_nexch[s];
+    }
+  }
+  if (tid < R) {
+    const int r = tid, ist = (rank * R + r) * nseq + iseq;
+    job.chi2c[ist] = s_chi2c[r];
+    job.flag[ist] = s_flag[r];
+    job.ptent[ist] = s_ptent[r];
+    job.ptentn[ist] = s_ptentn[r];
+    if (rng.inj) {
+      job.inj_cur[2 * ist] = rng.cu;
+      job.inj_cur[2 * ist + 1] = rng.cn;
+    } else {
+      reinterpret_cast<curandStateXORWOW *>(job.rndst)[ist] = rng.st;
+    }
+    if (rng.ovf) set_status(job.status, CMC_ERR_STREAM);
+  }
+  // Model rows of each replica's last evaluation (datm / chi2m outputs).
+  Model::template final_rows<R>(cta, plast, s_evald);
+  // No CTA may leave while another can still read its shared memory.
+  cluster.sync();
+}
+
+}  // namespace cmc

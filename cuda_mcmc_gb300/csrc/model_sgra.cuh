@@ -1,0 +1,441 @@
+// model_sgra.cuh -- built-in fast path for the Sgr A* crescent + Gaussian
+// visibility model: amplitudes (pass 0) and closure phases (pass 1).
+//
+// Same model as the reference's examples/sgra_model_fit/model.cuh:
+//   sgra_model9  (imodel == 1)  :322-462   Zsp Re rq ecc fade gax aq gq th
+//   sgra_model13 (imodel == 2)  :120-315   Zsp Re rq ecc fade gr gax aq gq
+//                                          alpha beta eta th
+//   model() dispatcher          :9-115     amplitude + phase for id < nvis,
+//                                          closures phi_i + phi_j - phi_k
+//                                          (cpExt 0) or from three model
+//                                          phases on a triangle (cpExt 1).
+//
+// Restated for the GPU:
+//   * The ring terms are written with F1(x) = J1(x)/x and F2(x) = J2(x)/x^2,
+//     both smooth even functions with finite limits at x = 0:
+//       ree = 0.5 (h+h0) Rex J1(x)/rho         = [0.5 (h+h0) Rex kex]   F1(x)
+//       ime = (h-h0)/(4 pi) [pi Rex (J0-J2)/rho^2 - J1/rho^3] U
+//           = -(h-h0)/(4 pi) x J2(x)/rho^3 U  = [-(h-h0)/(4 pi) kex^3] F2(x) U
+//     with x = kex rho, kex = 2 pi Rex (J0 - J2 = 2 J0 - 2 J1/x).  This removes
+//     the reference's rho <= 1e-7 branch (model.cuh:389-417): its limits are
+//     F1(0) = 1/2 and F2(0) = 1/8.
+//   * All parameter-only quantities (h, h0, d, rotations, weights, ...) are
+//     computed once per proposal per replica (prepare) instead of per datum.
+//   * Closure phases are formed from unit phasors z = V/|V| of the model:
+//     the residual wrap(obs - (phi_i + phi_j - phi_k)) equals
+//     arg(e^{i obs} conj(z_i z_j conj z_k)), one atan2 per closure.  When
+//     the phasors do not fit in shared memory, phases are stored instead
+//     and the residual is wrapped arithmetically.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "cmc_job.h"
+
+namespace cmc {
+
+struct SgraConsts {
+  float cth, sth;   // rotation by th
+  float kex, kin;   // 2 pi Rex, 2 pi Rin (nrad)
+  float ae, be;     // outer ring: ree = ae F1(kex rho), ime = be F2(kex rho) U
+  float ai, bi;     // inner ring
+  float dsh;        // inner-ring displacement phase / pi = dsh * U
+  float gc, gs;     // Gaussian axes rotation
+  float gx, gy;     // Gaussian exponent coefficients
+  float gpu, gpv;   // Gaussian phase / pi = gpu u + gpv v
+  float zr, zg;     // ring and Gaussian weights
+  int inner, gauss, ring;
+};
+
+// F1(x) = J1(x)/x and F2(x) = J2(x)/x^2.  Power series below x = 1 (terms
+// (-1)^m x^2m / (2^(2m+1) m! (m+1)!) and (-1)^m x^2m / (4^(m+1) m! (m+2)!));
+// above, from CUDA's j0f/j1f with J2 = 2 J1/x - J0.
+__device__ __forceinline__ void bessel_f12(float x, float &f1, float &f2)
+{
+  if (x < 1.0f) {
+    const float t = x * x;
+    f1 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.0f / 1474560.0f, -1.0f / 18432.0f),
+                              1.0f / 384.0f), -0.0625f), 0.5f);
+    f2 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.0f / 17694720.0f, -1.0f / 184320.0f),
+                              1.0f / 3072.0f), -1.0f / 96.0f), 0.125f);
+  } else {
+    const float ix = 1.0f / x;
+    const float j0 = j0f(x), j1 = j1f(x);
+    f1 = j1 * ix;
+    f2 = (2.0f * f1 - j0) * ix * ix;
+  }
+}
+
+__device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, float u, float v, float rho)
+{
+  float vre = 0.0f, vim = 0.0f;
+  if (c.ring) {
+    const float U = fmaf(u, c.cth, v * c.sth);
+    float f1, f2;
+    bessel_f12(c.kex * rho, f1, f2);
+    float re = c.ae * f1, im = c.be * f2 * U;
+    if (c.inner) {
+      float g1, g2, sd, cd;
+      bessel_f12(c.kin * rho, g1, g2);
+      const float rei = c.ai * g1, imi = c.bi * g2 * U;
+      sincospif(c.dsh * U, &sd, &cd);
+      re -= rei * cd - imi * sd;
+      im -= rei * sd + imi * cd;
+    }
+    vre = c.zr * re;
+    vim = c.zr * im;
+  }
+  if (c.gauss) {
+    const float ug = fmaf(u, c.gc, v * c.gs), vg = fmaf(v, c.gc, -u * c.gs);
+    const float ga = c.zg * expf(-fmaf(c.gx * ug, ug, c.gy * vg * vg));
+    float sg, cg;
+    sincospif(fmaf(c.gpu, u, c.gpv * v), &sg, &cg);
+    vre = fmaf(ga, cg, vre);
+    vim = fmaf(ga, sg, vim);
+  }
+  return make_float2(vre, vim);
+}
+
+__global__ void sgra_pack_kernel(const float *coor, const float *dat, const float *std2r,
+                                 const int *icoor, int nvis, int ncph, int cpext,
+                                 float4 *vis, int4 *cli, float4 *clf, int *status);
+
+struct SgraModel {
+  using Consts = SgraConsts;
+  struct Packed {
+    const float4 *vis;   // [npts]: u, v, amp_obs, 1/sigma^2 (0 for triangle points)
+    const int4 *cli;     // [ncph]: point indices i, j, k
+    const float4 *clf;   // [ncph]: cos obs, sin obs, 1/sigma^2, obs
+    int nvis, npts, ncph, cpext, npass, imodel, phasor, ndat;
+  };
+
+  static constexpr bool kRowsInEval = false;
+
+  __host__ __device__ static unsigned scratch_bytes(const Packed &pk, int R)
+  {
+    return (unsigned)R * (unsigned)pk.npts * (pk.phasor ? 8u : 4u);
+  }
+
+  // ---- host side: sizes, validation, packing ------------------------------
+  // mode 0: sweep, 1: calc_modchi2, 2: calc_model.
+  static int host_dims(const cmc_job &j, int mode, Packed &pk, const char **err)
+  {
+    const int nrep = j.nbeta * j.nseq;
+    pk.nvis = j.hidat[0];
+    pk.cpext = (j.nidat >= 3 && mode != 2) ? j.hidat[2] : 0;
+    pk.ncph = (mode == 2) ? 0 : j.ndat - pk.nvis;
+    pk.npass = (mode == 0) ? j.npass : 2;
+    pk.imodel = j.imodel;
+    pk.ndat = j.ndat;
+    if (pk.npass < 2) pk.ncph = 0;   // closures are a pass-1 product
+    pk.npts = pk.nvis + (pk.cpext ? 3 * pk.ncph : 0);
+    pk.phasor = 1;
+    if (j.nidat < 1 || pk.nvis < 0 || pk.nvis > j.ndat) {
+      *err = "Sgr A* model: idat[0] (nvis) must be in [0, ndat]";
+      return CMC_ERR_ARG;
+    }
+    if (j.imodel != 1 && j.imodel != 2) {
+      *err = "Sgr A* model: imodel must be 1 (sgra_model9) or 2 (sgra_model13)";
+      return CMC_ERR_MODEL;
+    }
+    if (j.nptot < (j.imodel == 1 ? 9 : 13)) {
+      *err = "Sgr A* model: nptot must be >= 9 (imodel 1) or >= 13 (imodel 2)";
+      return CMC_ERR_ARG;
+    }
+    if (pk.cpext) {
+      if (j.ncoor < 2 * pk.nvis + 4 * pk.ncph) {
+        *err = "Sgr A* model: cpExt=1 needs ncoor >= 2*nvis + 4*ncph";
+        return CMC_ERR_ARG;
+      }
+    } else {
+      if (j.ncoor < 2 * pk.nvis || (pk.npass >= 2 && j.nicoor < 3 * pk.ncph)) {
+        *err = "Sgr A* model: needs ncoor >= 2*nvis and nicoor >= 3*ncph";
+        return CMC_ERR_ARG;
+      }
+    }
+    const long long need = (long long)nrep * (j.ndat + pk.nvis);
+    if (j.datm != nullptr && j.ndatm < need) {
+      *err = "Sgr A* model: ndatm must be >= nbeta*nseq*(ndat + nvis) (amplitude/closure "
+             "head plus the phase tail)";
+      return CMC_ERR_ARG;
+    }
+    return CMC_OK;
+  }
+
+  static size_t host_work_bytes(const Packed &pk)
+  {
+    return (size_t)pk.npts * 16 + (size_t)pk.ncph * 32 + 64;
+  }
+
+  static int host_pack(const cmc_job &j, Packed &pk, void *work, cudaStream_t s)
+  {
+    unsigned char *w = (unsigned char *)work;
+    size_t o = 0;
+    pk.vis = (const float4 *)(w + o); o += ((size_t)pk.npts * 16 + 15) & ~(size_t)15;
+    pk.cli = (const int4 *)(w + o);   o += (size_t)pk.ncph * 16;
+    pk.clf = (const float4 *)(w + o);
+    const int n = pk.npts + pk.ncph;
+    if (n == 0) return CMC_OK;
+    int blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    sgra_pack_kernel<<<blocks, 256, 0, s>>>(j.coor, j.dat, j.std2r, j.icoor, pk.nvis, pk.ncph,
+                                            pk.cpext, (float4 *)pk.vis, (int4 *)pk.cli,
+                                            (float4 *)pk.clf, j.status);
+    return cudaGetLastError() == cudaSuccess ? CMC_OK : CMC_ERR_CUDA;
+  }
+
+  template <class Cta>
+  __device__ static void setup(Cta &, int, int) {}
+
+  template <class Cta>
+  __device__ static void after_exchange(Cta &) {}
+
+  template <class Cta>
+  __device__ static void prepare(Cta &cta, int r, const float *p)
+  {
+    SgraConsts &c = cta.consts[r];
+    const float pi = 3.1415926535897931f;
+    const int im = cta.pk->imodel;
+    const float Zsp = p[0], Re = p[1], rq = p[2], ecc = p[3], fade = p[4];
+    float gr = 0.f, gax, aq, gq, alpha = 0.f, beta = 0.f, eta = 0.f, th;
+    if (im == 1) {
+      gax = p[5]; aq = p[6]; gq = p[7]; th = p[8];
+    } else {
+      gr = p[5]; gax = p[6]; aq = p[7]; gq = p[8];
+      alpha = p[9]; beta = p[10]; eta = p[11]; th = p[12];
+    }
+    const float Rex = (pi / 180.0f) * (Re / 3600.0f) * 1e3f;   // uas -> nrad
+    const float Rin = rq * Rex;
+    float d = ecc * (Rex - Rin);
+    if (im != 1) d *= cosf(eta - th);
+    const float h = (2.0f / pi) / ((Rex * Rex - Rin * Rin * (1.0f + d / Rex)) * fade
+                                   + (Rex * Rex - Rin * Rin * (1.0f - d / Rex)));
+    const float h0 = fade * h;
+    sincosf(th, &c.sth, &c.cth);
+    c.kex = 2.0f * pi * Rex;
+    c.kin = 2.0f * pi * Rin;
+    c.ae = 0.5f * (h + h0) * Rex * c.kex;
+    c.be = -(h - h0) / (4.0f * pi) * (c.kex * c.kex * c.kex);
+    c.inner = (Rin != 0.0f);
+    c.ai = 0.5f * (h + h0 - d * (h - h0) / Rex) * Rin * c.kin;
+    c.bi = -(h - h0) / (4.0f * pi) * rq * (c.kin * c.kin * c.kin);
+    c.dsh = 2.0f * d;
+    // 2 (pi / (2 sqrt(2 ln 2)))^2 = pi^2 / (4 ln 2): FWHM^2 -> Gaussian exponent
+    const float gcoef = 3.5597039f;
+    const float gsy = gax * Rex, gsx = aq * gsy;
+    c.gx = gcoef * gsx * gsx;
+    c.gy = gcoef * gsy * gsy;
+    c.gauss = !(gax == 0.0f || aq == 0.0f || gq == 0.0f);
+    if (im == 1) {
+      const float gshift = Rin - d;
+      c.gc = c.cth;
+      c.gs = c.sth;
+      c.gpu = -2.0f * gshift * c.cth;
+      c.gpv = -2.0f * gshift * c.sth;
+    } else {
+      float sa, ca;
+      sincosf(beta, &c.gs, &c.gc);
+      sincosf(alpha, &sa, &ca);
+      c.gpu = -2.0f * gr * Rex * ca;
+      c.gpv = -2.0f * gr * Rex * sa;
+    }
+    if (c.gauss) {
+      c.zr = Zsp * (1.0f - gq);
+      c.zg = Zsp * gq;
+    } else {
+      c.zr = Zsp;
+      c.zg = 0.0f;
+    }
+    c.ring = 1;
+    if (im != 1 && gq == 1.0f) {   // sgra_model13: Gaussian only (model.cuh:204-210)
+      c.ring = 0;
+      c.zg = Zsp;
+      c.gauss = !(gax == 0.0f || aq == 0.0f);
+    }
+  }
+
+  // chi^2 of every active replica over all data (both passes).
+  template <int R, class Cta>
+  __device__ static void eval(Cta &cta, float (&acc)[R])
+  {
+    const Packed &pk = *cta.pk;
+    const int tid = cta.tid, T = cta.nthreads, npts = pk.npts;
+    bool act[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      acc[r] = 0.0f;
+      act[r] = cta.flag[r] != 0;
+    }
+    float2 *z = reinterpret_cast<float2 *>(cta.scratch);
+    float *ph = cta.scratch;
+    for (int i = tid; i < npts; i += T) {
+      const float4 d = __ldg(&pk.vis[i]);
+      const float rho = sqrtf(fmaf(d.x, d.x, d.y * d.y));
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (!act[r]) continue;
+        const float2 V = sgra_vis(cta.consts[r], d.x, d.y, rho);
+        const float n2 = fmaf(V.x, V.x, V.y * V.y);
+        const float amp = sqrtf(n2);
+        const float dif = d.z - amp;
+        acc[r] = fmaf(dif * dif, d.w, acc[r]);
+        if (pk.phasor) {
+          float2 zz = make_float2(1.0f, 0.0f);
+          if (n2 > 0.0f) {
+            const float rs = rsqrtf(n2);
+            zz = make_float2(V.x * rs, V.y * rs);
+          }
+          z[r * npts + i] = zz;
+        } else {
+          ph[r * npts + i] = atan2f(V.y, V.x);
+        }
+      }
+    }
+    if (pk.ncph == 0 || pk.npass < 2) return;
+    __syncthreads();
+    for (int c = tid; c < pk.ncph; c += T) {
+      const int4 q = __ldg(&pk.cli[c]);
+      const float4 f = __ldg(&pk.clf[c]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (!act[r]) continue;
+        float dif;
+        if (pk.phasor) {
+          const float2 a = z[r * npts + q.x], b = z[r * npts + q.y], e = z[r * npts + q.z];
+          // m = a * b * conj(e): model closure phasor
+          const float abr = a.x * b.x - a.y * b.y, abi = a.x * b.y + a.y * b.x;
+          const float mr = abr * e.x + abi * e.y, mi = abi * e.x - abr * e.y;
+          // residual phasor e^{i obs} * conj(m)
+          dif = atan2f(f.y * mr - f.x * mi, f.x * mr + f.y * mi);
+        } else {
+          const float x = f.w - (ph[r * npts + q.x] + ph[r * npts + q.y] - ph[r * npts + q.z]);
+          dif = x - 6.2831853071795865f * rintf(x * 0.15915494309189535f);
+        }
+        acc[r] = fmaf(dif * dif, f.z, acc[r]);
+      }
+    }
+  }
+
+  // calc_model (pass 0 only): amplitudes into datm[ist*ndat + i] and phases
+  // into the tail datm[nchi2m + ist*nvis + i] (src/gpu_mcmc.cu:633-658).
+  template <int R, class Cta>
+  __device__ static void model_rows(Cta &cta, const int *flags)
+  {
+    const cmc_job &job = *cta.job;
+    const Packed &pk = *cta.pk;
+    const int tid = cta.tid, T = cta.nthreads, nvis = pk.nvis, ndat = pk.ndat;
+    const size_t nchi2m = (size_t)job.nbeta * job.nseq * ndat;
+    for (int i = tid; i < nvis; i += T) {
+      const float4 d = __ldg(&pk.vis[i]);
+      const float rho = sqrtf(fmaf(d.x, d.x, d.y * d.y));
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (!flags[r]) continue;
+        const size_t ist = (size_t)cta.ist[r];
+        const float2 V = sgra_vis(cta.consts[r], d.x, d.y, rho);
+        job.datm[ist * ndat + i] = sqrtf(fmaf(V.x, V.x, V.y * V.y));
+        job.datm[nchi2m + ist * nvis + i] = atan2f(V.y, V.x);
+      }
+    }
+  }
+
+  // datm / chi2m rows of each replica's last evaluation, reference layout:
+  // datm[ist*ndat + id] amplitudes and closures, datm[nchi2m + ist*nvis + i]
+  // phases (model.cuh:38-43), chi2m[ist*ndat + id] terms (gpu_mcmc.cu:305-323).
+  template <int R, class Cta>
+  __device__ static void final_rows(Cta &cta, const float *plast, const int *evald)
+  {
+    const cmc_job &job = *cta.job;
+    const Packed &pk = *cta.pk;
+    if (job.datm == nullptr || job.chi2m == nullptr) return;
+    const int tid = cta.tid, T = cta.nthreads, npts = pk.npts, nvis = pk.nvis;
+    const int ndat = pk.ndat, nptot = job.nptot;
+    const size_t nchi2m = (size_t)job.nbeta * job.nseq * ndat;
+    float *ph = cta.scratch;   // phases [R][npts]
+    __syncthreads();
+    if (tid < R && evald[tid]) prepare(cta, tid, plast + tid * nptot);
+    __syncthreads();
+    for (int i = tid; i < npts; i += T) {
+      const float4 d = __ldg(&pk.vis[i]);
+      const float rho = sqrtf(fmaf(d.x, d.x, d.y * d.y));
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (!evald[r]) continue;
+        const float2 V = sgra_vis(cta.consts[r], d.x, d.y, rho);
+        const float amp = sqrtf(fmaf(V.x, V.x, V.y * V.y));
+        const float phase = atan2f(V.y, V.x);
+        ph[r * npts + i] = phase;
+        if (i < nvis) {
+          const size_t ist = (size_t)cta.ist[r];
+          const float dif = d.z - amp;
+          job.datm[ist * ndat + i] = amp;
+          job.datm[nchi2m + ist * nvis + i] = phase;
+          job.chi2m[ist * ndat + i] = (dif * dif) * d.w;
+        }
+      }
+    }
+    if (pk.ncph == 0 || pk.npass < 2) return;
+    __syncthreads();
+    for (int c = tid; c < pk.ncph; c += T) {
+      const int4 q = __ldg(&pk.cli[c]);
+      const float4 f = __ldg(&pk.clf[c]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (!evald[r]) continue;
+        const size_t ist = (size_t)cta.ist[r];
+        const float cph = ph[r * npts + q.x] + ph[r * npts + q.y] - ph[r * npts + q.z];
+        const float m = atan2f(sinf(cph), cosf(cph));
+        float dif = f.w - m;
+        dif = atan2f(sinf(dif), cosf(dif));
+        job.datm[ist * ndat + nvis + c] = m;
+        job.chi2m[ist * ndat + nvis + c] = (dif * dif) * f.z;
+      }
+    }
+  }
+};
+
+#ifndef CMC_INSTANCE_TU
+// Repack the reference-layout Sgr A* data (coor = [u0,v0,u1,v1,...] plus,
+// for cpExt == 1, [u1,v1,u2,v2] per closure; dat = [amp..., cph...];
+// std2r; icoor triplets) into the fast path's arrays.  Triangle points of
+// cpExt == 1 become extra points with zero amplitude weight.
+__global__ void sgra_pack_kernel(const float *coor, const float *dat, const float *std2r,
+                                 const int *icoor, int nvis, int ncph, int cpext,
+                                 float4 *vis, int4 *cli, float4 *clf, int *status)
+{
+  const int npts = nvis + (cpext ? 3 * ncph : 0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npts + ncph;
+       i += gridDim.x * blockDim.x) {
+    if (i < nvis) {
+      vis[i] = make_float4(coor[2 * i], coor[2 * i + 1], dat[i], std2r[i]);
+    } else if (i < npts) {
+      const int c = (i - nvis) / 3, t = (i - nvis) - 3 * c;
+      const int o = 2 * nvis + 4 * c;
+      float u, v;
+      if (t == 0) { u = coor[o]; v = coor[o + 1]; }
+      else if (t == 1) { u = coor[o + 2]; v = coor[o + 3]; }
+      else { u = -(coor[o] + coor[o + 2]); v = -(coor[o + 1] + coor[o + 3]); }
+      vis[i] = make_float4(u, v, 0.0f, 0.0f);
+    } else {
+      const int c = i - npts;
+      int a, b, e;
+      if (cpext) {
+        a = nvis + 3 * c; b = a + 1; e = a + 2;
+      } else {
+        a = icoor[3 * c]; b = icoor[3 * c + 1]; e = icoor[3 * c + 2];
+        if (a < 0 || a >= nvis || b < 0 || b >= nvis || e < 0 || e >= nvis) {
+          if (status) atomicCAS(status, 0, (int)CMC_ERR_ARG);
+          a = b = e = 0;
+        }
+      }
+      const float obs = dat[nvis + c];
+      float so, co;
+      sincosf(obs, &so, &co);
+      cli[c] = make_int4(a, b, e, 0);
+      clf[c] = make_float4(co, so, std2r[nvis + c], obs);
+    }
+  }
+}
+
+#endif  // CMC_INSTANCE_TU
+
+}  // namespace cmc

@@ -1,0 +1,216 @@
+"""Device-resident sampler jobs: the C-ABI's ``cmc_run`` / ``cmc_eval`` on
+arrays that stay in GPU memory (PyTorch tensors used as plain device buffers).
+
+A :class:`DeviceJob` holds one problem (data + parameter description) and
+the full sampler state in the reference's layouts.  ``run()`` launches the
+fused sweep for any number of burn-in / main iterations and can resume from
+the current state, so long runs can be split into chunks (and captured in
+CUDA graphs) without changing the chain: a run split into chunks walks the
+same chain as one launch over all iterations.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_F32, _I32, _U8 = torch.float32, torch.int32, torch.uint8
+
+# state arrays copied back by to_numpy(), in the reference's shapes
+STATE_FIELDS = ("pcur", "chi2c", "flag", "ptent", "ptentn", "pstp", "n_acpt", "n_exch",
+                "n_cnt", "n_hist", "tcur", "rndst", "pout", "tout", "chi2", "datm", "chi2m")
+
+
+def sampler_defaults(pdescr, pmint, pmaxt, nbeta, nseq, nadj=100, ptotal=None, pstp=None):
+    """Initial state as imgpu.Mcgpu builds it (src/imgpu.py:320-424): ivar /
+    invar maps, pcur at the prior centres (ptotal for frozen parameters),
+    pstp = (pmax - pmin)/50 unless given, tcur = 0..nbeta-1 per sequence,
+    n_cnt = 1 and zeroed counters."""
+    pdescr = np.ascontiguousarray(pdescr, np.int32)
+    nptot = pdescr.size
+    pmint = np.ascontiguousarray(pmint, np.float32)
+    pmaxt = np.ascontiguousarray(pmaxt, np.float32)
+    ivar = np.where(pdescr != 0)[0].astype(np.int32)
+    nprm = ivar.size
+    invar = np.full(nptot, -1, np.int32)
+    invar[ivar] = np.arange(nprm, dtype=np.int32)
+    ptotal = np.zeros(nptot, np.float32) if ptotal is None else np.asarray(ptotal, np.float32)
+    pcur = np.empty((nbeta, nseq, nptot), np.float32)
+    pcur[:] = ptotal
+    pcur[:, :, ivar] = pmint[ivar] + (pmaxt[ivar] - pmint[ivar]) / np.float32(2.0)
+    st = np.empty((nprm, nbeta, nseq), np.float32)
+    if pstp is None:
+        st[:] = ((pmaxt[ivar] - pmint[ivar]) / 50.0).astype(np.float32)[:, None, None]
+    else:
+        p = np.asarray(pstp, np.float32)
+        st[:] = p.reshape(nprm, 1, 1) if p.size == nprm else p.reshape(nprm, nbeta, nseq)
+    tcur = np.empty((nbeta, nseq), np.int32)
+    tcur[:] = np.arange(nbeta, dtype=np.int32)[:, None]
+    return dict(pdescr=pdescr, ivar=ivar, invar=invar, ptotal=ptotal, pmint=pmint, pmaxt=pmaxt,
+                pcur=pcur, pstp=st, tcur=tcur,
+                chi2c=np.zeros((nbeta, nseq), np.float32),
+                flag=np.zeros((nbeta, nseq), np.int32),
+                ptent=np.zeros((nbeta, nseq), np.float32),
+                ptentn=np.zeros((nbeta, nseq), np.int32),
+                n_acpt=np.zeros((nprm, nbeta, nseq), np.int32),
+                n_exch=np.zeros((nbeta, nseq), np.int32),
+                n_cnt=np.ones((nprm, nbeta, nseq), np.int32),
+                n_hist=np.zeros((nadj, nprm, nbeta, nseq), np.int32))
+
+
+def _dev(a, dtype, device):
+    return torch.as_tensor(np.ascontiguousarray(a)).to(device=device, dtype=dtype).contiguous()
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else C.c_void_p(0)
+
+
+class DeviceJob:
+    """One MCMC-RE problem with all arrays resident on ``device``.
+
+    rng = "curand" uses the reference's generator (curand_init(seed, ist, 0));
+    rng = "injected" reads uniforms / normals from ``streams = (u, n)``,
+    float32 arrays [nbeta*nseq, L] consumed in the reference's draw order.
+    """
+
+    def __init__(self, model, coor, dat, std2r, icoor, idat, pdescr, pmint, pmaxt, beta,
+                 nseq, niter_total, imodel=1, npass=1, nadj=100, ptotal=None, pstp=None,
+                 seed=1234, rng="curand", streams=None, ndatm=None, device="cuda",
+                 lib=None):
+        self.L = lib if lib is not None else _lib.load(model)
+        self.device = torch.device(device)
+        d = self.device
+        beta = np.ascontiguousarray(beta, np.float32)
+        self.nbeta, self.nseq = int(beta.size), int(nseq)
+        nrep = self.nbeta * self.nseq
+        s = sampler_defaults(pdescr, pmint, pmaxt, self.nbeta, self.nseq, nadj, ptotal, pstp)
+        self.nptot, self.nprm, self.nadj = int(s["pdescr"].size), int(s["ivar"].size), int(nadj)
+        self.ndat = int(np.asarray(dat).size)
+        idat = np.ascontiguousarray(idat, np.int32)
+        nvis = int(idat[0]) if model == "sgra" else 0
+        self.nvis = nvis
+        self.ndatm = int(ndatm) if ndatm is not None else nrep * (self.ndat + nvis)
+        self.niter_total = int(niter_total)
+        icoor = np.ascontiguousarray(icoor, np.int32)
+        if icoor.size == 0:
+            icoor = np.zeros(1, np.int32)
+        t = {}
+        t["coor"] = _dev(coor, _F32, d)
+        t["dat"] = _dev(dat, _F32, d)
+        t["std2r"] = _dev(std2r, _F32, d)
+        t["icoor"] = _dev(icoor, _I32, d)
+        t["idat"] = _dev(idat, _I32, d)
+        for k in ("pdescr", "ivar", "invar"):
+            t[k] = _dev(s[k], _I32, d)
+        for k in ("pmint", "pmaxt"):
+            t[k] = _dev(s[k], _F32, d)
+        t["beta"] = _dev(beta, _F32, d)
+        for k in ("pcur", "chi2c", "ptent", "pstp"):
+            t[k] = _dev(s[k], _F32, d)
+        for k in ("flag", "ptentn", "n_acpt", "n_exch", "n_cnt", "n_hist", "tcur"):
+            t[k] = _dev(s[k], _I32, d)
+        t["rndst"] = torch.zeros((self.nbeta, self.nseq, 48), dtype=_U8, device=d)
+        nt = max(self.niter_total, 1)
+        t["pout"] = torch.zeros((self.nprm, self.nbeta, self.nseq, nt), dtype=_F32, device=d)
+        t["tout"] = torch.zeros((self.nbeta, self.nseq, nt), dtype=_I32, device=d)
+        t["chi2"] = torch.zeros((self.nseq, nt), dtype=_F32, device=d)
+        t["datm"] = torch.zeros(max(self.ndatm, 1), dtype=_F32, device=d)
+        t["chi2m"] = torch.zeros((self.nbeta, self.nseq, self.ndat), dtype=_F32, device=d)
+        t["status"] = torch.zeros(4, dtype=_I32, device=d)
+        self.rng = rng
+        if rng == "injected":
+            if streams is None:
+                raise ValueError("rng='injected' needs streams=(u, n)")
+            u, n = streams
+            t["inj_u"] = _dev(u, _F32, d)
+            t["inj_n"] = _dev(n, _F32, d)
+            t["inj_cur"] = torch.zeros((nrep, 2), dtype=_I32, device=d)
+        elif rng != "curand":
+            raise ValueError("rng must be 'curand' or 'injected'")
+        self.t = t
+        j = _lib.CmcJob()
+        j.ncoor, j.ndat, j.nicoor, j.nidat = int(t["coor"].numel()), self.ndat, \
+            int(icoor.size), int(idat.size)
+        j.ndatm, j.nptot, j.nprm, j.nadj = self.ndatm, self.nptot, self.nprm, self.nadj
+        j.npass, j.nbeta, j.nseq, j.imodel = int(npass), self.nbeta, self.nseq, int(imodel)
+        j.niter_total = self.niter_total
+        j.rng_mode = _lib.CMC_RNG_INJECTED if rng == "injected" else _lib.CMC_RNG_CURAND
+        j.seed = int(np.uint64(seed))
+        for i in range(4):
+            j.hidat[i] = int(idat[i]) if i < idat.size else 0
+        for k in ("coor", "dat", "std2r", "icoor", "idat", "pdescr", "ivar", "invar", "pmint",
+                  "pmaxt", "beta", "pcur", "chi2c", "flag", "ptent", "ptentn", "pstp", "n_acpt",
+                  "n_exch", "n_cnt", "n_hist", "tcur", "rndst", "pout", "tout", "chi2", "datm",
+                  "chi2m", "status"):
+            setattr(j, k, _ptr(t[k]))
+        if rng == "injected":
+            j.inj_u, j.inj_n, j.inj_cur = _ptr(t["inj_u"]), _ptr(t["inj_n"]), _ptr(t["inj_cur"])
+            j.inj_lu, j.inj_ln = int(t["inj_u"].shape[1]), int(t["inj_n"].shape[1])
+        wb = int(self.L.cmc_work_bytes(C.byref(j), 0))
+        t["work"] = torch.zeros(max(wb, 16), dtype=_U8, device=d)
+        j.work, j.work_bytes = _ptr(t["work"]), wb
+        self.job = j
+        self.itr_done = 0
+
+    @classmethod
+    def from_workload(cls, w, niter_total=None, seed=1234, rng="curand", streams=None,
+                      device="cuda", lib=None):
+        return cls(w.model, w.coor, w.dat, w.std2r, w.icoor, w.idat, w.pdescr, w.pmint, w.pmaxt,
+                   w.beta(), w.nseq, w.niter if niter_total is None else niter_total,
+                   imodel=w.imodel, npass=w.npass, ptotal=w.ptotal, pstp=w.pstp0, seed=seed,
+                   rng=rng, streams=streams, device=device, lib=lib)
+
+    # ---- launching -----------------------------------------------------------
+    def run(self, nburn=0, niter=0, do_init=False, itr0=None, stream=None):
+        """Launch the fused sweep on ``stream`` (torch's current stream by
+        default).  Main iterations are recorded from column ``itr0`` (default:
+        after the previously recorded ones).  Asynchronous: call
+        :meth:`check` to synchronise and read the device status."""
+        j = self.job
+        j.do_init = 1 if do_init else 0
+        j.nburn, j.niter = int(nburn), int(niter)
+        j.itr0 = self.itr_done if itr0 is None else int(itr0)
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(self.L, self.L.cmc_run(C.byref(j), C.c_void_p(s.cuda_stream)))
+        self.itr_done = j.itr0 + j.niter
+
+    def eval(self, mode=_lib.MODE_MODCHI2, stream=None):
+        """calc_modchi2 (mode 1) / calc_model (mode 2) on the current pcur."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(self.L, self.L.cmc_eval(C.byref(self.job), int(mode),
+                                           C.c_void_p(s.cuda_stream)))
+
+    def check(self):
+        torch.cuda.synchronize(self.device)
+        st = int(self.t["status"][0].item())
+        if st:
+            raise _lib.McmcError(st, "device status %d (see cmc_status in cmc_job.h)" % st)
+
+    def config(self):
+        """Launch shape the library picks for this job: (R, G, T, phasor, smem, clusters/wave)."""
+        R, G, T, P, W = (C.c_int() for _ in range(5))
+        sm = C.c_size_t()
+        _lib.check(self.L, self.L.cmc_query_config(C.byref(self.job), C.byref(R), C.byref(G),
+                                                   C.byref(T), C.byref(P), C.byref(sm),
+                                                   C.byref(W)))
+        return dict(R=R.value, G=G.value, T=T.value, phasor=P.value, smem=sm.value,
+                    clusters_per_wave=W.value)
+
+    # ---- state access ----------------------------------------------------------
+    def to_numpy(self, fields=STATE_FIELDS):
+        torch.cuda.synchronize(self.device)
+        out = {k: self.t[k].cpu().numpy() for k in fields}
+        if self.rng == "injected":
+            out["inj_cur"] = self.t["inj_cur"].cpu().numpy()
+        return out
+
+    def set_state(self, **arrays):
+        """Overwrite device state arrays from host arrays of the same shapes."""
+        for k, v in arrays.items():
+            dst = self.t[k]
+            src = torch.as_tensor(np.ascontiguousarray(v)).to(dtype=dst.dtype).reshape(dst.shape)
+            dst.copy_(src.to(self.device))
