@@ -1,0 +1,398 @@
+"""Benchmark: chi^2 model evaluations per second of the MCMC-RE sweep.
+
+Workload (default): the Sgr A* crescent + Gaussian fit, sgra_model9 on
+seeded synthetic data with 2000 visibility amplitudes + 600 closure phases,
+64 sequences x 32 temperatures (2048 replicas), 9 mutable parameters.  One
+"step" is one sweep chunk of 500 iterations (100 burn-in + 400 main, the
+1:4 ratio of the full 5000 + 20000 run) over all replicas:
+500 * 9 * 2048 = 9,216,000 chi^2 evaluations, each over all 2600 data.
+
+  value  -- device-resident inputs, the fused sweep via cmc_run (resumed
+            chunk after chunk, as a long run is split);
+  e2e    -- the reference-facing call mcmc_cuda (host buffers, H2D + D2H
+            copies inside the timed region) per step;
+  cpu_baseline -- the CPU oracle port of the sweep (FP64 model) on a bounded
+            sample, all host threads;
+  roofline -- the sweep kernel's achieved FP32 rate from the algorithmic
+            FLOP count per evaluation against a measured FP32 (SGEMM) peak.
+
+Run: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic work per chi^2 evaluation of sgra_model9 (frozen op-count
+# convention: FADD/FMUL = 1, FFMA = 2 FLOP; Bessel J0/J1 as degree-5/5
+# rationals): 180 FLOP per amplitude term, 25 FLOP per closure term.
+FLOP_PER_AMP, FLOP_PER_CPH = 180.0, 25.0
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--burn-per-step", type=int, default=100)
+    ap.add_argument("--main-per-step", type=int, default=400)
+    ap.add_argument("--nvis", type=int, default=2000)
+    ap.add_argument("--ncph", type=int, default=600)
+    ap.add_argument("--nseq", type=int, default=64)
+    ap.add_argument("--nbeta", type=int, default=32)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(args, rank=0):
+    from cuda_mcmc_gb300 import synth
+    return synth.sgra(nvis=args.nvis, ncph=args.ncph, seed=3, nseq=args.nseq, nbeta=args.nbeta,
+                      nburn=args.burn_per_step, niter=args.main_per_step)
+
+
+def evals_per_step(w, args):
+    return (args.burn_per_step + args.main_per_step) * w.nprm * w.nbeta * w.nseq
+
+
+def flop_per_eval(w):
+    return w.nvis * FLOP_PER_AMP + (w.ndat - w.nvis) * FLOP_PER_CPH
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp32_peak_tflops():
+    """Measured FP32 SIMT peak: cuBLAS SGEMM (TF32 off), best of 5."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    torch.matmul(a, b)
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle port of the sweep, parallel over sequences
+# ---------------------------------------------------------------------------
+
+class CpuSweep:
+    """The oracle port of the sweep (FP64 model) on all w.nseq sequences,
+    split over `threads` host threads: sequences are independent (the replica
+    exchange stays inside a sequence), so each thread owns a group of them.
+    ctypes releases the GIL, so the threads run in parallel."""
+
+    def __init__(self, w, threads, max_iters, seed=1):
+        import oracle
+        self.oracle = oracle
+        self.w = w
+        self.pb = oracle.Problem(w.model, w.coor, w.dat, w.std2r, w.icoor, w.idat, w.nptot,
+                                 w.imodel, w.npass)
+        self.jobs = []
+        for i, g in enumerate([list(range(i, w.nseq, threads))
+                               for i in range(min(threads, w.nseq))]):
+            ns = len(g)
+            st = oracle.new_state(w.pdescr, w.pmint, w.pmaxt, w.beta(), ns, 1, ptotal=w.ptotal,
+                                  ndat=w.ndat)
+            rs = oracle.make_streams(ns * w.nbeta,
+                                     w.nprm * (3 * max_iters + 2) + 3 * w.nbeta * max_iters + 64,
+                                     w.nprm * max_iters + 8, seed + i)
+            self.jobs.append((st, rs, ns))
+        self._parallel(1, 0)                      # init_pcur + first chi^2
+
+    def _parallel(self, do_init, iters):
+        ths = [threading.Thread(target=self.oracle.sweep,
+                                args=(self.pb, st, rs, do_init, iters, 0))
+               for (st, rs, _) in self.jobs]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+
+    def step(self, iters):
+        t0 = time.perf_counter()
+        self._parallel(0, iters)
+        dt = time.perf_counter() - t0
+        return iters * self.w.nprm * self.w.nbeta * self.w.nseq, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    w = workload(args)
+    threads = os.cpu_count() or 1
+    cpu = CpuSweep(w, threads, args.warmup + args.steps, seed=100)
+    rates = []
+    for i in range(args.warmup + args.steps):
+        ev, dt = cpu.step(1)
+        if i >= args.warmup:
+            rates.append((ev, dt))
+    tot_ev = sum(x[0] for x in rates)
+    tot_t = sum(x[1] for x in rates)
+    val = tot_ev / tot_t
+    line = {
+        "impl": "reference", "metric": "chi2 model evals/sec", "value": val,
+        "unit": "chi2 evals/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot_t / len(rates), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sgra9 %dvis+%dcph, %dx%d replicas" % (
+            w.nvis, w.ndat - w.nvis, w.nseq, w.nbeta),
+            "step": "1 MCMC-RE iteration (9 proposals + exchange) of all replicas",
+            "parallelism": "replicas only"},
+        "cpu_baseline": {"value": val, "unit": "chi2 evals/s", "cores": threads, "kind": "port",
+                         "sample": "%d iterations x %d replicas, oracle sweep (FP64 model), "
+                                   "sequences split over %d threads" % (
+                                       args.steps, w.nseq * w.nbeta, threads)},
+        "e2e": {"value": val, "unit": "chi2 evals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def e2e_rate(w, args, steps, warmup):
+    """mcmc_cuda with host numpy buffers, one full call per step."""
+    import torch
+    from cuda_mcmc_gb300 import mcmc_interf
+    from cuda_mcmc_gb300.device import sampler_defaults
+    mcmc_interf.use_model("sgra")
+    nrep, nprm = w.nbeta * w.nseq, w.nprm
+    nb, ni = args.burn_per_step, args.main_per_step
+    s0 = sampler_defaults(w.pdescr, w.pmint, w.pmaxt, w.nbeta, w.nseq)
+    beta = w.beta()
+
+    def call(seed):
+        s = {k: v.copy() for k, v in s0.items()}
+        pout = np.empty((nprm, w.nbeta, w.nseq, ni), np.float32)
+        tout = np.empty((w.nbeta, w.nseq, ni), np.int32)
+        chi2 = np.empty((w.nseq, ni), np.float32)
+        datm = np.zeros(nrep * (w.ndat + w.nvis), np.float32)
+        chi2m = np.zeros((w.nbeta, w.nseq, w.ndat), np.float32)
+        rndst = np.zeros((w.nbeta, w.nseq, 48), np.uint8)
+        mcmc_interf.mcmcuda(w.coor, w.dat, w.std2r, w.icoor, w.idat, datm, chi2m, s["pdescr"],
+                            s["ivar"], s["invar"], s["ptotal"], s["pmint"], s["pmaxt"], pout,
+                            tout, chi2, s["chi2c"], s["tcur"], s["flag"], s["n_acpt"],
+                            s["n_exch"], s["n_cnt"], s["n_hist"], beta, s["pstp"], s["ptent"],
+                            s["ptentn"], s["pcur"], rndst, np.uint64(seed), w.imodel,
+                            w.coor.size, w.ndat, w.icoor.size, w.idat.size, datm.size, w.nptot,
+                            nprm, 100, w.npass, w.nbeta, w.nseq, nb, ni)
+        return s, pout, tout, chi2, datm, chi2m, rndst
+
+    for i in range(warmup):
+        call(1000 + i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        out = call(2000 + i)
+    dt = time.perf_counter() - t0
+    s = out[0]
+    h2d = sum(a.nbytes for a in (w.coor, w.dat, w.std2r, w.icoor, w.idat, s["pdescr"], s["ivar"],
+                                 s["invar"], s["pmint"], s["pmaxt"], s["tcur"], s["flag"],
+                                 s["chi2c"], s["n_acpt"], s["n_exch"], s["n_cnt"], s["n_hist"],
+                                 beta, s["pstp"], s["ptent"], s["ptentn"], s["pcur"]))
+    d2h = sum(a.nbytes for a in out[1:]) + sum(
+        s[k].nbytes for k in ("tcur", "n_acpt", "n_cnt", "n_exch", "n_hist", "pstp", "ptent",
+                              "ptentn", "pcur", "flag", "chi2c"))
+    return evals_per_step(w, args) * steps / dt, dt / steps, h2d, d2h
+
+
+def run_mine(args, rank, world, local):
+    import torch
+    from cuda_mcmc_gb300 import _lib
+    from cuda_mcmc_gb300.device import DeviceJob
+    _lib.load("sgra")
+    w = workload(args, rank)
+    job = DeviceJob.from_workload(w, niter_total=args.main_per_step, seed=1234 + rank)
+    cfg = job.config()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    job.run(0, 0, do_init=True)
+    job.check()
+    for _ in range(args.warmup):
+        job.run(args.burn_per_step, args.main_per_step, itr0=0)
+        flush.zero_()
+    job.check()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            job.run(args.burn_per_step, args.main_per_step, itr0=0, stream=stream)
+            evs[i][1].record(stream)
+            flush.zero_()
+        torch.cuda.synchronize()
+        barrier(world)
+        dt = time.perf_counter() - t0
+    job.check()
+    dt = max_over_ranks(dt, world)
+    kern_s = [a.elapsed_time(b) / 1e3 for a, b in evs]
+    n_ev = evals_per_step(w, args)
+    value = n_ev * args.steps * world / dt
+    if rank != 0:
+        return
+    clocks = clk.summary()
+    avg_launch = float(np.mean(kern_s))
+    peak = fp32_peak_tflops()
+    achieved = n_ev * flop_per_eval(w) / avg_launch / 1e12
+    line = {
+        "metric": "chi2 model evals/sec", "value": value, "unit": "chi2 evals/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {
+            "workload": "sgra9 %dvis+%dcph, %dx%d replicas" % (w.nvis, w.ndat - w.nvis, w.nseq,
+                                                                w.nbeta),
+            "step": "%d burn-in + %d main iterations (9 proposals + exchange each) of all "
+                    "replicas = %d chi2 evals" % (args.burn_per_step, args.main_per_step, n_ev),
+            "parallelism": "replicas only (independent sequences per GPU)",
+            "l2": "2x L2 buffer written between timed steps",
+            "launch": cfg},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured cuBLAS SGEMM (TF32 off) in this run",
+                     "flop_per_eval": flop_per_eval(w)},
+        "clocks": clocks,
+        "gpu_launches": 2 * args.steps,
+    }
+    if not args.no_e2e and world == 1:
+        e2e, e2e_step, h2d, d2h = e2e_rate(w, args, steps=args.steps, warmup=1)
+        line["e2e"] = {"value": e2e, "unit": "chi2 evals/s", "h2d_bytes_per_step": h2d,
+                       "d2h_bytes_per_step": d2h, "s_per_step": e2e_step,
+                       "call": "mcmc_cuda (host buffers, one call per step incl. init)"}
+    if not args.no_cpu and world == 1:
+        threads = os.cpu_count() or 1
+        cev, cdt = CpuSweep(w, threads, 1).step(1)
+        r = cev / cdt
+        line["cpu_baseline"] = {"value": r, "unit": "chi2 evals/s", "cores": threads,
+                                "kind": "port",
+                                "sample": "1 iteration x %d replicas (%d evals, %.1f s), oracle "
+                                          "sweep with FP64 model, sequences over %d threads" % (
+                                              w.nseq * w.nbeta, cev, cdt, threads)}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_mine(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

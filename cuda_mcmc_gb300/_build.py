@@ -21,6 +21,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 MODELS_DIR = os.path.join(PKG, "models")
 LIB_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(PKG, "_lib", "obj")
@@ -38,15 +39,16 @@ def nvcc() -> str:
 
 def _flags():
     return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-            "-I", CSRC, "--expt-relaxed-constexpr"]
+            "-I", CSRC, "-I", INCLUDE, "--expt-relaxed-constexpr"]
 
 
 def _sources_digest(extra=()):
     h = hashlib.sha1()
-    for name in sorted(os.listdir(CSRC)):
-        with open(os.path.join(CSRC, name), "rb") as f:
-            h.update(name.encode())
-            h.update(f.read())
+    for d in (CSRC, INCLUDE):
+        for name in sorted(os.listdir(d)):
+            with open(os.path.join(d, name), "rb") as f:
+                h.update(name.encode())
+                h.update(f.read())
     for p in extra:
         with open(p, "rb") as f:
             h.update(f.read())

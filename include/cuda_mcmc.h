@@ -1,0 +1,132 @@
+/*
+ * cuda_mcmc.h -- C-ABI of the GB300 MCMC-RE sweep libraries.
+ *
+ * Every model library (libcmc_sgra.so for the built-in Sgr A* model,
+ * libcmc_<name>.so for a model.cuh plugin) exports exactly these symbols.
+ * All arguments are plain pointers and sizes.
+ *
+ * Entry points that replace the reference's (MITHaystack/cuda_mcmc,
+ * src/mcmc.h:7-32, implemented in src/mcmcjob.cu:227-298 and :475-545):
+ * identical signatures, argument meaning, array layouts and in-place output
+ * semantics.  The arrays are caller-owned HOST buffers; the call copies them
+ * to the device, runs, and writes every output back into the same buffers.
+ * Where the reference reports a CUDA error by printing and calling exit(1)
+ * (src/mcmcjob.cu:212-219), these print to stderr and return; the _v2
+ * variants return the status instead (see cmc_last_error()).
+ */
+#ifndef CUDA_MCMC_H
+#define CUDA_MCMC_H
+
+#include <stddef.h>
+
+#include "cmc_job.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Replaces mcmc_cuda, src/mcmc.h:7-20 / src/mcmcjob.cu:475-545: the full
+ * burn-in + main-stage MCMC-RE run (run_mcmc, src/gpu_mcmc.cu:682-763).
+ * Inputs: coor, dat, std2r, icoor, idat, pdescr, ivar, invar, ptotal, pmint,
+ * pmaxt, beta and the starting tcur, flag, n_acpt, n_exch, n_cnt, n_hist, pstp,
+ * ptent, ptentn, pcur (mutable parameters are re-drawn from the prior, as
+ * init_pcur does).  Outputs (in place): pout [nprm][nbeta][nseq][niter],
+ * tout [nbeta][nseq][niter], chi2 [nseq][niter], the final sampler state
+ * (pcur, chi2c, flag, tcur, pstp, ptent, ptentn, n_acpt, n_exch, n_cnt,
+ * n_hist, rndst = cuRAND XORWOW states, 48 bytes per replica) and the model
+ * rows datm / chi2m of each replica's last evaluation. */
+void mcmc_cuda(float *coor, float *dat, float *std2r, int *icoor, int *idat, float *datm,
+               float *chi2m, int *pdescr, int *ivar, int *invar, float *ptotal, float *pmint,
+               float *pmaxt, float *pout, int *tout, float *chi2, float *chi2c, int *tcur,
+               int *flag, int *n_acpt, int *n_exch, int *n_cnt, int *n_hist, float *beta,
+               float *pstp, float *ptent, int *ptentn, float *pcur, unsigned char *rndst,
+               unsigned long long seed, int imodel, int ncoor, int ndat, int nicoor, int nidat,
+               int ndatm, int nptot, int nprm, int nadj, int npass, int nbeta, int nseq,
+               int nburn, int niter);
+
+/* Replaces calc_modchi2, src/mcmc.h:23-27 / src/mcmcjob.cu:227-254 (the
+ * header names the 17th int nprm, the definition nptot; it is nptot): model
+ * values datm, chi^2 terms chi2m and chi2c = sum of each chi2m row for the
+ * nbeta*nseq parameter sets in pcur whose flag is non-zero (two passes, as
+ * run_calcmodchi2, src/gpu_mcmc.cu:769-783). */
+void calc_modchi2(float *coor, float *dat, float *std2r, int *icoor, int *idat, float *datm,
+                  float *chi2m, float *pcur, float *chi2c, int *flag, int imodel, int ncoor,
+                  int ndat, int nicoor, int nidat, int ndatm, int nptot, int nbeta, int nseq);
+
+/* Replaces calc_model, src/mcmc.h:30-32 / src/mcmcjob.cu:257-298: model
+ * values only (pass 0, run_calcmodel, src/gpu_mcmc.cu:790-802) for every
+ * parameter set in pcur (the reference leaves its flag array uninitialised;
+ * here every set is evaluated). */
+void calc_model(float *coor, int *idat, float *datm, float *pcur, int imodel, int ncoor,
+                int ndat, int nidat, int ndatm, int nptot, int nbeta, int nseq);
+
+/* Same arguments as the three above; return a cmc_status (0 = success).
+ * Reference counterparts: mcmc_cuda / calc_modchi2 / calc_model, whose
+ * failure path is CUDA_CALL -> cudaAssert -> exit(1) (src/mcmcjob.cuh:6). */
+int mcmc_cuda_v2(float *coor, float *dat, float *std2r, int *icoor, int *idat, float *datm,
+                 float *chi2m, int *pdescr, int *ivar, int *invar, float *ptotal, float *pmint,
+                 float *pmaxt, float *pout, int *tout, float *chi2, float *chi2c, int *tcur,
+                 int *flag, int *n_acpt, int *n_exch, int *n_cnt, int *n_hist, float *beta,
+                 float *pstp, float *ptent, int *ptentn, float *pcur, unsigned char *rndst,
+                 unsigned long long seed, int imodel, int ncoor, int ndat, int nicoor, int nidat,
+                 int ndatm, int nptot, int nprm, int nadj, int npass, int nbeta, int nseq,
+                 int nburn, int niter);
+int calc_modchi2_v2(float *coor, float *dat, float *std2r, int *icoor, int *idat, float *datm,
+                    float *chi2m, float *pcur, float *chi2c, int *flag, int imodel, int ncoor,
+                    int ndat, int nicoor, int nidat, int ndatm, int nptot, int nbeta, int nseq);
+int calc_model_v2(float *coor, int *idat, float *datm, float *pcur, int imodel, int ncoor,
+                  int ndat, int nidat, int ndatm, int nptot, int nbeta, int nseq);
+
+/* Message of the last failed call on this thread ("" after a success).
+ * The reference prints "Cuda error in file ..." (src/mcmcjob.cu:212-219). */
+const char *cmc_last_error(void);
+
+/* Replaces reset_gpu, src/mcmc_interf.pyx:342-343 (cudaDeviceReset): waits
+ * for the device instead of destroying the context other libraries share.
+ * Returns a cmc_status. */
+int cmc_reset_gpu(void);
+
+/* ---- device-pointer API: the same sweep on arrays already in GPU memory ----
+ * Reference counterpart: CMcmcFit::do_mcmc_on_gpu -> run_mcmc
+ * (src/mcmcjob.cu:835-848, src/gpu_mcmc.cu:682-763) on the device copies that
+ * the CMcmcFit constructor made (src/mcmcjob.cu:552-755); here the caller owns
+ * the device arrays (see cmc_job in cmc_job.h).  A job can run in chunks:
+ * do_init = 0 resumes from the state arrays (including the generator states),
+ * and main iteration m of a launch is recorded at column itr0 + m.  Launches
+ * are asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream);
+ * the kernels report device-side failures in job->status. */
+int cmc_run(const cmc_job *job, void *stream);
+
+/* Reference counterpart: run_calcmodchi2 / run_calcmodel
+ * (src/gpu_mcmc.cu:769-802) on device arrays: mode 1 = calc_modchi2,
+ * mode 2 = calc_model.  Asynchronous on `stream`. */
+int cmc_eval(const cmc_job *job, int mode, void *stream);
+
+/* Bytes of library scratch (packed data of the built-in fast models) that
+ * job->work must provide for cmc_run (mode 0) or cmc_eval (mode 1, 2).  The
+ * reference allocates its device buffers itself (src/mcmcjob.cu:689-718). */
+size_t cmc_work_bytes(const cmc_job *job, int mode);
+
+/* Launch shape the library picks for a cmc_run of this job: replicas per
+ * CTA R, cluster size G = nbeta/R, threads per CTA T, closure storage
+ * (1 = unit phasors, 0 = phases), dynamic shared memory and resident
+ * clusters per wave.  The reference always launches <<<nseq, nbeta>>> per
+ * step kernel and <<<nbeta*nseq*ndat/128+1, 128>>> for the model
+ * (src/gpu_mcmc.cu:686-687). */
+int cmc_query_config(const cmc_job *job, int *R, int *G, int *T, int *phasor, size_t *smem,
+                     int *clusters_per_wave);
+
+/* Force a launch shape (0 / -1 = automatic), e.g. from the autotuner.  No
+ * reference counterpart (the reference's shape is fixed). */
+void cmc_set_config(int R, int T, int phasor);
+
+/* Library identification; no reference counterpart. */
+const char *cmc_model_name(void);
+int cmc_abi_version(void);
+int cmc_sizeof_job(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUDA_MCMC_H */

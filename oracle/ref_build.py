@@ -32,6 +32,14 @@ MODELS = {"sgra": "examples/sgra_model_fit",
           "solvsys": "examples/solvsys"}
 
 
+def _host_has_fma() -> bool:
+    try:
+        with open("/proc/cpuinfo") as f:
+            return " fma " in f.read()
+    except OSError:
+        return False
+
+
 def available() -> bool:
     return os.path.isfile(os.path.join(REF_ROOT, "src", "gpu_mcmc.cu"))
 
@@ -45,7 +53,11 @@ def build(force: bool = False) -> list:
         return []
     os.makedirs(OUT, exist_ok=True)
     src = os.path.join(REF_ROOT, "src")
-    flags = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w",
+    # nvcc contracts a*b + c into fused multiply-adds by default (-fmad=true);
+    # -ffp-contract=fast with FMA instructions gives the host build the same
+    # single-rounding proposal step p + pstp*N(0,1) as the reference's GPU build.
+    fma = ["-mfma"] if _host_has_fma() else []
+    flags = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=fast", *fma, "-w",
              "-I", SHIM, "-I", src, "-include", os.path.join(SHIM, "kernel_env.h")]
     drv = os.path.join(OUT, "ref_driver.o")
     drv_src = os.path.join(HERE, "ref_driver.cpp")

@@ -1,0 +1,319 @@
+"""Parity of the CUDA path (through the C-ABI) with the oracle and the
+reference's own code.
+
+Tolerances (float32 kernels against the FP64 oracle):
+  * model amplitudes: |err| <= 1e-5 |V| + 1e-6 Zsp.  The absolute part is a
+    few float32 ulps of the zero-spacing flux Zsp: near a visibility null the
+    amplitude is a float32 sum of O(Zsp) terms that cancel, so no float32
+    evaluation (the reference's own included) is relatively accurate there;
+  * model phases: |err| <= 2e-5 + 1e-6 Zsp/|V| rad (the phase error an
+    amplitude-scale error of 1e-6 Zsp makes); closure phases: 1e-4 rad;
+  * chi^2 of a parameter set: relative 1e-5;
+  * decisions (accept / reject / swap): identical, except a decision whose
+    uniform draw lies within 1e-3*alpha of its acceptance probability alpha
+    (a near tie that float32 chi^2 may legitimately flip).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden
+from cuda_mcmc_gb300 import _lib, mcmc_interf, synth
+from cuda_mcmc_gb300.device import DeviceJob
+
+pytestmark = pytest.mark.gpu
+
+AMP_RTOL, AMP_ATOL, PHASE_ATOL, CPH_ATOL = 1e-5, 1e-6, 2e-5, 1e-4
+CHI2_RTOL, TIE_RTOL = 1e-5, 1e-3
+
+
+def _wrap(x):
+    return np.angle(np.exp(1j * x))
+
+
+def _pb(w):
+    return oracle.Problem(w.model, w.coor, w.dat, w.std2r, w.icoor, w.idat, w.nptot, w.imodel,
+                          w.npass)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _libs():
+    for m in ("sgra", "rosenbrock", "solvsys", "nlsys"):
+        _lib.load(m)
+
+
+# ---------------------------------------------------------------------------
+# model + chi^2 (calc_modchi2 / calc_model through the host C-ABI)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("name", ["sgra_modchi2_m9.npz", "sgra_modchi2_m13.npz",
+                                  "sgra_modchi2_cpext.npz"])
+def test_calc_modchi2_sgra(name):
+    g = golden(name)
+    mcmc_interf.use_model("sgra")
+    P = g["pcur"]
+    nrep, nptot = P.shape
+    nvis, ndat = int(g["idat"][0]), g["dat"].size
+    datm = np.zeros(nrep * (ndat + nvis), np.float32)
+    chi2m = np.zeros((nrep, 1, ndat), np.float32)
+    chi2c = np.zeros((nrep, 1), np.float32)
+    flag = np.ones((nrep, 1), np.int32)
+    mcmc_interf.calcmodchi2(g["coor"], g["dat"], g["std2r"], g["icoor"], g["idat"], datm, chi2m,
+                            P.reshape(nrep, 1, nptot).copy(), chi2c, flag, int(g["imodel"]),
+                            g["coor"].size, ndat, g["icoor"].size, 3, datm.size, nptot, nrep, 1)
+    pb = oracle.Problem("sgra", g["coor"], g["dat"], g["std2r"], g["icoor"], g["idat"], nptot,
+                        int(g["imodel"]), 2)
+    d, ph, c2m, c2 = oracle.calc_modchi2(pb, P)
+    gd = datm[:nrep * ndat].reshape(nrep, ndat)
+    gph = datm[nrep * ndat:].reshape(nrep, nvis)
+    zsp = P[:, :1]
+    amp_err = np.abs(gd[:, :nvis] - d[:, :nvis]) - AMP_RTOL * np.abs(d[:, :nvis])
+    assert amp_err.max() <= AMP_ATOL * zsp.min()
+    ph_tol = PHASE_ATOL + AMP_ATOL * zsp / np.maximum(np.abs(d[:, :nvis]), 1e-30)
+    assert np.all(np.abs(_wrap(gph - ph)) <= ph_tol)
+    assert np.abs(_wrap(gd[:, nvis:] - d[:, nvis:])).max() < CPH_ATOL
+    assert np.max(np.abs(chi2c.ravel() - c2) / c2) < CHI2_RTOL
+    # chi2c is the sum of its chi2m row, as in the reference (calc_chi2)
+    assert np.allclose(chi2m.reshape(nrep, ndat).sum(1), chi2c.ravel(), rtol=1e-5)
+    # and the reference's own float32 numbers agree to float32 accuracy
+    assert np.max(np.abs(chi2c.ravel() - g["chi2c"]) / g["chi2c"]) < CHI2_RTOL
+
+
+def test_calc_model_sgra():
+    w = synth.sgra(nvis=300, ncph=0, seed=9, nseq=1, nbeta=1)
+    rng = np.random.default_rng(3)
+    P = rng.uniform(synth.SGRA9_PMIN, synth.SGRA9_PMAX, (8, 9)).astype(np.float32)
+    nrep, nvis = 8, 300
+    idat = np.array([nvis, 0, 0], np.int32)
+    datm = np.zeros(nrep * 2 * nvis, np.float32)
+    mcmc_interf.use_model("sgra")
+    mcmc_interf.calcmodel(w.coor, idat, datm, P.reshape(nrep, 1, 9).copy(), 1, w.coor.size,
+                          nvis, 3, datm.size, 9, nrep, 1)
+    amp, ph = datm[:nrep * nvis].reshape(nrep, nvis), datm[nrep * nvis:].reshape(nrep, nvis)
+    for r in range(nrep):
+        a, p = oracle.sgra_vis(1, P[r], w.coor[0::2], w.coor[1::2])
+        assert np.max(np.abs(amp[r] - a) - AMP_RTOL * a) <= AMP_ATOL * P[r, 0]
+        assert np.all(np.abs(_wrap(ph[r] - p)) <= PHASE_ATOL + AMP_ATOL * P[r, 0] / a)
+
+
+@pytest.mark.parametrize("w", [synth.rosenbrock(n=4), synth.solvsys(), synth.nlsys()],
+                         ids=["rosenbrock", "solvsys", "nlsys"])
+def test_calc_modchi2_plugins(w):
+    mcmc_interf.use_model(w.model)
+    rng = np.random.default_rng(5)
+    nrep = 64
+    P = rng.uniform(w.pmint, w.pmaxt, (nrep, w.nptot)).astype(np.float32)
+    datm = np.zeros(nrep * w.ndat, np.float32)
+    chi2m = np.zeros((nrep, 1, w.ndat), np.float32)
+    chi2c = np.zeros((nrep, 1), np.float32)
+    mcmc_interf.calcmodchi2(w.coor, w.dat, w.std2r, w.icoor, w.idat, datm, chi2m,
+                            P.reshape(nrep, 1, -1).copy(), chi2c, np.ones((nrep, 1), np.int32),
+                            0, w.coor.size, w.ndat, w.icoor.size, w.idat.size, datm.size,
+                            w.nptot, nrep, 1)
+    _, _, _, c2 = oracle.calc_modchi2(_pb(w), P)
+    assert np.max(np.abs(chi2c.ravel() - c2) / np.maximum(c2, 1e-6)) < CHI2_RTOL
+
+
+# ---------------------------------------------------------------------------
+# the sweep
+# ---------------------------------------------------------------------------
+
+def _golden_job(model):
+    g = golden("sweep_%s.npz" % model)
+    job = DeviceJob(model, g["coor"], g["dat"], g["std2r"], g["icoor"], g["idat"], g["pdescr"],
+                    g["pmint"], g["pmaxt"], g["beta"], int(g["nseq"]), int(g["niter"]),
+                    imodel=int(g["imodel"]), npass=int(g["npass"]), ptotal=g["ptotal"],
+                    pstp=g["pstp0"], rng="injected", streams=(g["u"], g["n"]))
+    return g, job
+
+
+@pytest.mark.parametrize("model", ["sgra", "rosenbrock", "solvsys"])
+def test_sweep_matches_reference_decision_for_decision(model):
+    """Injected streams: the fused kernel takes every accept / reject / swap
+    decision of the reference's own kernels (golden fixtures)."""
+    g, job = _golden_job(model)
+    job.run(int(g["nburn"]), int(g["niter"]), do_init=True)
+    job.check()
+    s = job.to_numpy()
+    for f in ("n_acpt", "n_exch", "n_cnt", "n_hist", "tcur", "tout", "flag", "ptentn"):
+        assert np.array_equal(s[f], g[f]), f
+    assert np.array_equal(s["inj_cur"][:, 0], g["cu"]) and np.array_equal(s["inj_cur"][:, 1], g["cn"])
+    assert np.allclose(s["pcur"], g["pcur"], rtol=1e-5, atol=1e-6)
+    assert np.allclose(s["pout"], g["pout"], rtol=1e-5, atol=1e-6)
+    assert np.allclose(s["pstp"], g["pstp"], rtol=1e-6, atol=0)
+    assert np.allclose(s["chi2"], g["chi2"], rtol=CHI2_RTOL, atol=1e-5)
+
+
+def _oracle_state_from(job_state, w, niter_total):
+    st = oracle.new_state(w.pdescr, w.pmint, w.pmaxt, w.beta(), w.nseq, niter_total,
+                          ptotal=w.ptotal, ndat=w.ndat)
+    for f in ("pcur", "flag", "ptent", "ptentn", "pstp", "n_acpt", "n_exch", "n_cnt", "n_hist",
+              "tcur"):
+        getattr(st, f)[...] = job_state[f]
+    st.chi2c = job_state["chi2c"].astype(np.float64)
+    return st
+
+
+@pytest.mark.parametrize("cfg", ["sgra", "nlsys", "rosenbrock"])
+def test_sweep_lockstep_vs_fp64_oracle(cfg):
+    """Larger data than the fixtures: from the same state and the same
+    injected draws, every iteration of the kernel makes the FP64 oracle's
+    decisions (near ties excepted) and reaches its chi^2 within 1e-5."""
+    if cfg == "sgra":
+        w = synth.sgra(nvis=400, ncph=120, seed=8, nseq=2, nbeta=8)
+    elif cfg == "nlsys":
+        w = synth.nlsys(nseq=2, nbeta=8)
+    else:
+        w = synth.rosenbrock(nseq=2, nbeta=8)
+    nburn, niter = 6, 6
+    nrep = w.nbeta * w.nseq
+    rs = oracle.make_streams(nrep, 4000, 1000, 77)
+    job = DeviceJob.from_workload(w, niter_total=niter, rng="injected", streams=(rs.u, rs.n))
+    job.run(0, 0, do_init=True)
+    job.check()
+    s = job.to_numpy()
+    st = oracle.new_state(w.pdescr, w.pmint, w.pmaxt, w.beta(), w.nseq, niter, ptotal=w.ptotal,
+                          ndat=w.ndat)
+    if w.pstp0 is not None:
+        st.pstp[:] = np.asarray(w.pstp0, np.float32)[:, None, None]
+    ors = oracle.Streams(rs.u, rs.n)
+    oracle.sweep(_pb(w), st, ors, 1, 0, 0)
+    assert np.allclose(s["pcur"], st.pcur, rtol=1e-6, atol=1e-7)
+    assert np.max(np.abs(s["chi2c"] - st.chi2c) / np.maximum(st.chi2c, 1e-6)) < CHI2_RTOL
+    mismatched = 0
+    for step in range(nburn + niter):
+        burn = step < nburn
+        st = _oracle_state_from(s, w, niter)
+        ors = oracle.Streams(rs.u, rs.n, s["inj_cur"][:, 0].copy(), s["inj_cur"][:, 1].copy())
+        tr = oracle.sweep(_pb(w), st, ors, 0, 1 if burn else 0, 0 if burn else 1, trace=True)
+        job.run(1 if burn else 0, 0 if burn else 1, itr0=0)
+        job.check()
+        s = job.to_numpy()
+        same = (np.array_equal(s["n_acpt"], st.n_acpt) and np.array_equal(s["n_exch"], st.n_exch)
+                and np.array_equal(s["tcur"], st.tcur) and np.array_equal(s["n_hist"], st.n_hist)
+                and np.array_equal(s["inj_cur"][:, 0], ors.cu))
+        if same:
+            assert np.allclose(s["pcur"], st.pcur, rtol=1e-6, atol=1e-7)
+            assert np.max(np.abs(s["chi2c"] - st.chi2c) / np.maximum(st.chi2c, 1e-6)) < CHI2_RTOL
+        else:
+            # allowed only when the oracle saw a near tie in this iteration
+            alpha_m = np.abs(tr.margin[tr.dec >= 0])
+            x_m = np.abs(tr.xmargin)
+            assert alpha_m.min(initial=1.0) < TIE_RTOL or x_m.min(initial=1.0) < TIE_RTOL
+            mismatched += 1
+    assert mismatched <= 1
+
+
+def test_mcmc_cuda_host_abi_equals_device_api():
+    """mcmc_interf.mcmcuda (host buffers, the reference's call) and a
+    device-resident job with the same seed produce identical outputs."""
+    w = synth.sgra(nvis=300, ncph=90, seed=12, nseq=4, nbeta=8, nburn=20, niter=30)
+    seed = 99
+    job = DeviceJob.from_workload(w, seed=seed)
+    job.run(w.nburn, w.niter, do_init=True)
+    job.check()
+    dev = job.to_numpy()
+    from cuda_mcmc_gb300.device import sampler_defaults
+    s = sampler_defaults(w.pdescr, w.pmint, w.pmaxt, w.nbeta, w.nseq)
+    nrep, nprm = w.nbeta * w.nseq, w.nprm
+    pout = np.zeros((nprm, w.nbeta, w.nseq, w.niter), np.float32)
+    tout = np.zeros((w.nbeta, w.nseq, w.niter), np.int32)
+    chi2 = np.zeros((w.nseq, w.niter), np.float32)
+    datm = np.zeros(nrep * (w.ndat + w.nvis), np.float32)
+    chi2m = np.zeros((w.nbeta, w.nseq, w.ndat), np.float32)
+    rndst = np.zeros((w.nbeta, w.nseq, 48), np.uint8)
+    mcmc_interf.use_model("sgra")
+    mcmc_interf.mcmcuda(w.coor, w.dat, w.std2r, w.icoor, w.idat, datm, chi2m, s["pdescr"],
+                        s["ivar"], s["invar"], s["ptotal"], s["pmint"], s["pmaxt"], pout, tout,
+                        chi2, s["chi2c"], s["tcur"], s["flag"], s["n_acpt"], s["n_exch"],
+                        s["n_cnt"], s["n_hist"], w.beta(), s["pstp"], s["ptent"], s["ptentn"],
+                        s["pcur"], rndst, np.uint64(seed), w.imodel, w.coor.size, w.ndat,
+                        w.icoor.size, w.idat.size, datm.size, w.nptot, nprm, 100, w.npass,
+                        w.nbeta, w.nseq, w.nburn, w.niter)
+    assert np.array_equal(pout, dev["pout"])
+    assert np.array_equal(tout, dev["tout"])
+    assert np.array_equal(chi2, dev["chi2"])
+    assert np.array_equal(rndst, dev["rndst"])
+    for f in ("pcur", "chi2c", "pstp", "n_acpt", "n_exch", "n_cnt", "n_hist", "tcur"):
+        assert np.array_equal(s[f], dev[f]), f
+    assert np.array_equal(datm, dev["datm"]) and np.array_equal(chi2m, dev["chi2m"])
+
+
+def test_chunked_run_equals_single_launch():
+    w = synth.nlsys(nseq=4, nbeta=8)
+    a = DeviceJob.from_workload(w, niter_total=40, seed=5)
+    a.run(30, 40, do_init=True)
+    b = DeviceJob.from_workload(w, niter_total=40, seed=5)
+    b.run(10, 0, do_init=True)
+    b.run(20, 15)
+    b.run(0, 25)
+    a.check()
+    b.check()
+    sa, sb = a.to_numpy(), b.to_numpy()
+    for f in ("pout", "tout", "chi2", "pcur", "chi2c", "rndst", "n_acpt", "n_hist", "pstp"):
+        assert np.array_equal(sa[f], sb[f]), f
+
+
+def test_chi2_trace_is_fp64_chi2_of_recorded_samples():
+    """Size-independent property at the benchmark's data size: every recorded
+    chi2[iseq, itr] is the chi^2 of the recorded coldest-slot sample."""
+    w = synth.sgra(nvis=2000, ncph=600, seed=3, nseq=8, nbeta=32, nburn=30, niter=40)
+    job = DeviceJob.from_workload(w, seed=2)
+    job.run(w.nburn, w.niter, do_init=True)
+    job.check()
+    s = job.to_numpy()
+    idx = [(q, it) for q in range(w.nseq) for it in range(0, w.niter, 13)]
+    P = np.stack([s["pout"][:, 0, q, it] for (q, it) in idx]).astype(np.float32)
+    _, _, _, c2 = oracle.calc_modchi2(_pb(w), P)
+    c2g = np.array([s["chi2"][q, it] for (q, it) in idx])
+    assert np.max(np.abs(c2g - c2) / c2) < CHI2_RTOL
+    # every tcur column is a permutation of 0..nbeta-1
+    assert all(sorted(s["tcur"][:, q]) == list(range(w.nbeta)) for q in range(w.nseq))
+    # each burn-in proposal counts one trial: sum_k n_cnt = nprm + nburn*nprm
+    assert np.all(s["n_cnt"].sum(0) == w.nprm * (1 + w.nburn))
+
+
+def test_known_answers_solvsys_and_rosenbrock():
+    w = synth.solvsys(nseq=14, nbeta=32, nburn=400, niter=5000)   # solvsys.py:38-40
+    job = DeviceJob.from_workload(w, seed=1)
+    job.run(w.nburn, w.niter, do_init=True)
+    job.check()
+    s = job.to_numpy()
+    chi2, pout = s["chi2"].ravel(), s["pout"][:, 0].reshape(2, -1)
+    rx = np.array([(-4.0 - np.sqrt(832.0)) / 34.0, (-4.0 + np.sqrt(832.0)) / 34.0])
+    best = pout[:, chi2 < 2e-4]
+    assert best.shape[1] > 0
+    d = np.min(np.abs(best[0][:, None] - rx[None, :]), axis=1)
+    assert np.all(d < 0.05)
+    # every hit sits on one of the two roots (a coldest chain need not visit both)
+    found = {int(np.argmin(np.abs(x - rx))) for x in best[0]}
+    assert found and found <= {0, 1}
+    w = synth.rosenbrock(n=4, nseq=16, nbeta=32, nburn=1000, niter=5000)
+    job = DeviceJob.from_workload(w, seed=2)
+    job.run(w.nburn, w.niter, do_init=True)
+    job.check()
+    s = job.to_numpy()
+    i = np.argmin(s["chi2"])
+    xbest = s["pout"][:, 0].reshape(4, -1)[:, i]
+    assert np.all(np.abs(xbest - 1.0) < 0.1)
+
+
+def test_errors_are_reported_not_faults():
+    w = synth.sgra(nvis=50, ncph=10, seed=1, nseq=1, nbeta=2, nburn=1, niter=1)
+    bad = w.icoor.copy()
+    bad[0] = 10 ** 6                        # closure index out of range
+    job = DeviceJob("sgra", w.coor, w.dat, w.std2r, bad, w.idat, w.pdescr, w.pmint, w.pmaxt,
+                    w.beta(), 1, 1, imodel=1, npass=2)
+    job.run(1, 1, do_init=True)
+    with pytest.raises(_lib.McmcError):
+        job.check()
+    job2 = DeviceJob.from_workload(w)
+    job2.job.imodel = 7
+    with pytest.raises(_lib.McmcError, match="imodel"):
+        job2.run(1, 1, do_init=True)
+    job3 = DeviceJob.from_workload(w)
+    job3.job.nbeta = 1
+    with pytest.raises(_lib.McmcError, match="nbeta"):
+        job3.run(1, 1, do_init=True)
