@@ -128,15 +128,15 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         });
         if (n <= 0) continue;
         const int waves = (j.nseq + n - 1) / n;
-        // prefer phasors (cheaper closures), then more threads per replica
-        const double score = (double)waves * R * (ph ? 1.0 : 1.15) * (T == 64 ? 1.1 : 1.0);
+        // makespan ~ waves * R; phasors make closures cheaper, and fewer
+        // threads per replica leave less parallelism per proposal
+        const double score = (double)waves * R * (ph ? 1.0 : 1.05) * (T == 64 ? 1.1 : 1.0);
         if (score < best - 1e-9) {
           best = score;
           out.R = R; out.G = G; out.T = T; out.phasor = ph; out.smem = smem;
           out.clusters_per_wave = n;
           found = true;
         }
-        break;   // the phasor variant fitted: no need to try phases
       }
     }
   }

@@ -1,0 +1,77 @@
+// fastmath.cuh -- float32 helpers for the model inner loops.
+//
+// Polynomial coefficients come from gen_fastmath.py / gen_bessel_table.py
+// (Chebyshev interpolants of float64 values); accuracies are a few float32
+// ulps, stated in the generated headers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "bessel_table.cuh"
+#include "fastmath_coef.cuh"
+
+namespace cmc {
+
+// sin(pi t), cos(pi t): t = n + r with n = rint(t), |r| <= 1/2, and
+// sin(pi (n + r)) = (-1)^n sin(pi r), cos(pi (n + r)) = (-1)^n cos(pi r).
+__device__ __forceinline__ void sincospi_poly(float t, float *s, float *c)
+{
+  const float n = rintf(t);
+  const float r = t - n;
+  const float q = r * r;
+  float ps = kSinPiS[5];
+#pragma unroll
+  for (int k = 4; k >= 0; --k) ps = fmaf(ps, q, kSinPiS[k]);
+  float pc = kCosPiK[6];
+#pragma unroll
+  for (int k = 5; k >= 0; --k) pc = fmaf(pc, q, kCosPiK[k]);
+  const float sg = (((int)n) & 1) ? -1.0f : 1.0f;
+  *s = sg * (ps * r);
+  *c = sg * pc;
+}
+
+// atan2(y, x) in [-pi, pi]: a = min/max of |x|, |y| in [0, 1], atan(a) from
+// the polynomial, then the octant.  atan2(0, 0) = 0.
+__device__ __forceinline__ float atan2_poly(float y, float x)
+{
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  const float a = (mx > 0.0f) ? __fdividef(mn, mx) : 0.0f;
+  const float s = a * a;
+  float p = kAtanP[9];
+#pragma unroll
+  for (int k = 8; k >= 0; --k) p = fmaf(p, s, kAtanP[k]);
+  float r = p * a;
+  if (ay > ax) r = 1.57079632679489662f - r;
+  if (x < 0.0f) r = 3.14159265358979324f - r;
+  return copysignf(r, y);
+}
+
+// F1(x) = J1(x)/x and F2(x) = J2(x)/x^2 (even in x) from the piecewise
+// polynomial table `tab` (a shared-memory copy of kBesselTab); beyond the
+// table, from CUDA's j0f/j1f with J2 = 2 J1/x - J0.
+__device__ __forceinline__ void bessel_f12_tab(const float2 *tab, float x, float &f1, float &f2)
+{
+  x = fabsf(x);
+  if (x < (float)kBesselIntervals) {
+    const int i = (int)x;
+    const float d = x - ((float)i + 0.5f);
+    const float2 *c = tab + i * (kBesselDeg + 1);
+    float2 a = c[kBesselDeg];
+    float p1 = a.x, p2 = a.y;
+#pragma unroll
+    for (int k = kBesselDeg - 1; k >= 0; --k) {
+      a = c[k];
+      p1 = fmaf(p1, d, a.x);
+      p2 = fmaf(p2, d, a.y);
+    }
+    f1 = p1;
+    f2 = p2;
+  } else {
+    const float ix = 1.0f / x;
+    const float j0 = j0f(x), j1 = j1f(x);
+    f1 = j1 * ix;
+    f2 = (2.0f * f1 - j0) * ix * ix;
+  }
+}
+
+}  // namespace cmc

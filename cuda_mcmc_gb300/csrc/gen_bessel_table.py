@@ -1,0 +1,102 @@
+"""Generate bessel_table.cuh: piecewise polynomials for
+    F1(x) = J1(x) / x      and      F2(x) = J2(x) / x^2
+on x in [0, XMAX) in unit intervals [i, i+1), each a degree-DEG polynomial in
+d = x - (i + 0.5).  Both functions are entire and even, with F1(0) = 1/2 and
+F2(0) = 1/8.
+
+Method: for every interval, interpolate the function at the DEG+1 Chebyshev
+points of the interval (values from SciPy's float64 Bessel functions), convert
+the Chebyshev interpolant to monomial coefficients in d (|d| <= 1/2, so the
+monomial form is well conditioned), and round to float32.  The script reports
+the maximum error of the float32 polynomials, evaluated with float32 Horner,
+against float64 values on a dense grid.
+
+    python cuda_mcmc_gb300/csrc/gen_bessel_table.py   # rewrites bessel_table.cuh
+"""
+import os
+
+import numpy as np
+from numpy.polynomial import chebyshev as Ch
+from numpy.polynomial import polynomial as Po
+from scipy.special import j1, jv
+
+XMAX = 16
+DEG = 9
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def f1(x):
+    x = np.asarray(x, np.float64)
+    out = np.empty_like(x)
+    small = np.abs(x) < 1e-4
+    out[small] = 0.5 - x[small] ** 2 / 16
+    out[~small] = j1(x[~small]) / x[~small]
+    return out
+
+
+def f2(x):
+    x = np.asarray(x, np.float64)
+    out = np.empty_like(x)
+    small = np.abs(x) < 1e-3
+    out[small] = 0.125 - x[small] ** 2 / 96
+    out[~small] = jv(2, x[~small]) / x[~small] ** 2
+    return out
+
+
+def fit(fun, i):
+    c = i + 0.5
+    # Chebyshev nodes on d in [-1/2, 1/2]
+    k = np.arange(DEG + 1)
+    t = np.cos((2 * k + 1) * np.pi / (2 * (DEG + 1)))
+    d = 0.5 * t
+    cc = Ch.chebfit(t, fun(c + d), DEG)          # interpolant in t = 2d
+    mono_t = Ch.cheb2poly(cc)                      # coefficients in t
+    mono_d = mono_t * (2.0 ** np.arange(DEG + 1))  # t = 2d
+    return mono_d.astype(np.float32)
+
+
+def horner32(coef, d):
+    d = np.float32(d)
+    acc = np.float32(coef[-1])
+    for a in coef[-2::-1]:
+        acc = np.float32(acc * d + np.float32(a))
+    return acc
+
+
+def main():
+    tab = np.zeros((XMAX, DEG + 1, 2), np.float32)
+    err = [0.0, 0.0]
+    for i in range(XMAX):
+        tab[i, :, 0] = fit(f1, i)
+        tab[i, :, 1] = fit(f2, i)
+        xs = np.linspace(i, i + 1, 401)[:-1]
+        for j, fun in enumerate((f1, f2)):
+            ref = fun(xs)
+            got = np.array([horner32(tab[i, :, j], np.float32(x) - np.float32(i + 0.5))
+                            for x in xs], np.float64)
+            err[j] = max(err[j], float(np.max(np.abs(got - ref))))
+    lines = [
+        "// bessel_table.cuh -- GENERATED by gen_bessel_table.py; do not edit.",
+        "//",
+        "// F1(x) = J1(x)/x and F2(x) = J2(x)/x^2 on [0, %d): interval i = [i, i+1) holds" % XMAX,
+        "// coefficients a_k (k = 0..%d) of sum_k a_k d^k, d = x - (i + 0.5), stored as" % DEG,
+        "// pairs (F1 a_k, F2 a_k).  Chebyshev interpolants of float64 values, rounded",
+        "// to float32; max |error| with float32 Horner: F1 %.2e, F2 %.2e." % tuple(err),
+        "#pragma once",
+        "",
+        "namespace cmc {",
+        "constexpr int kBesselIntervals = %d;" % XMAX,
+        "constexpr int kBesselDeg = %d;" % DEG,
+        "static __device__ const float2 kBesselTab[%d][%d] = {" % (XMAX, DEG + 1),
+    ]
+    for i in range(XMAX):
+        row = ", ".join("{%.9ef, %.9ef}" % (tab[i, k, 0], tab[i, k, 1]) for k in range(DEG + 1))
+        lines.append("    {%s}," % row)
+    lines += ["};", "}  // namespace cmc", ""]
+    with open(os.path.join(HERE, "bessel_table.cuh"), "w") as f:
+        f.write("\n".join(lines))
+    print("max abs error: F1 %.3e  F2 %.3e" % tuple(err))
+
+
+if __name__ == "__main__":
+    main()

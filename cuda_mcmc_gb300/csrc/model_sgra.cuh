@@ -21,6 +21,10 @@
 //     F1(0) = 1/2 and F2(0) = 1/8.
 //   * All parameter-only quantities (h, h0, d, rotations, weights, ...) are
 //     computed once per proposal per replica (prepare) instead of per datum.
+//   * F1/F2 come from piecewise polynomial tables (bessel_table.cuh); the
+//     data points are packed sorted by |uv|, so the 32 lanes of a warp read
+//     the same (or two neighbouring) table intervals for any replica.
+//   * sin/cos of pi*t and atan2 are float32 polynomials (fastmath.cuh).
 //   * Closure phases are formed from unit phasors z = V/|V| of the model:
 //     the residual wrap(obs - (phi_i + phi_j - phi_k)) equals
 //     arg(e^{i obs} conj(z_i z_j conj z_k)), one atan2 per closure.  When
@@ -29,7 +33,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "cmc_job.h"
+#include "fastmath.cuh"
 
 namespace cmc {
 
@@ -46,38 +53,21 @@ struct SgraConsts {
   int inner, gauss, ring;
 };
 
-// F1(x) = J1(x)/x and F2(x) = J2(x)/x^2.  Power series below x = 1 (terms
-// (-1)^m x^2m / (2^(2m+1) m! (m+1)!) and (-1)^m x^2m / (4^(m+1) m! (m+2)!));
-// above, from CUDA's j0f/j1f with J2 = 2 J1/x - J0.
-__device__ __forceinline__ void bessel_f12(float x, float &f1, float &f2)
-{
-  if (x < 1.0f) {
-    const float t = x * x;
-    f1 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.0f / 1474560.0f, -1.0f / 18432.0f),
-                              1.0f / 384.0f), -0.0625f), 0.5f);
-    f2 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.0f / 17694720.0f, -1.0f / 184320.0f),
-                              1.0f / 3072.0f), -1.0f / 96.0f), 0.125f);
-  } else {
-    const float ix = 1.0f / x;
-    const float j0 = j0f(x), j1 = j1f(x);
-    f1 = j1 * ix;
-    f2 = (2.0f * f1 - j0) * ix * ix;
-  }
-}
-
-__device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, float u, float v, float rho)
+// Model visibility V = Vre + i Vim of one replica at (u, v), |uv| = rho.
+__device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, const float2 *btab, float u,
+                                          float v, float rho)
 {
   float vre = 0.0f, vim = 0.0f;
   if (c.ring) {
     const float U = fmaf(u, c.cth, v * c.sth);
     float f1, f2;
-    bessel_f12(c.kex * rho, f1, f2);
+    bessel_f12_tab(btab, c.kex * rho, f1, f2);
     float re = c.ae * f1, im = c.be * f2 * U;
     if (c.inner) {
       float g1, g2, sd, cd;
-      bessel_f12(c.kin * rho, g1, g2);
+      bessel_f12_tab(btab, c.kin * rho, g1, g2);
       const float rei = c.ai * g1, imi = c.bi * g2 * U;
-      sincospif(c.dsh * U, &sd, &cd);
+      sincospi_poly(c.dsh * U, &sd, &cd);
       re -= rei * cd - imi * sd;
       im -= rei * sd + imi * cd;
     }
@@ -86,33 +76,43 @@ __device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, float u, float v
   }
   if (c.gauss) {
     const float ug = fmaf(u, c.gc, v * c.gs), vg = fmaf(v, c.gc, -u * c.gs);
-    const float ga = c.zg * expf(-fmaf(c.gx * ug, ug, c.gy * vg * vg));
+    const float ga = c.zg * __expf(-fmaf(c.gx * ug, ug, c.gy * vg * vg));
     float sg, cg;
-    sincospif(fmaf(c.gpu, u, c.gpv * v), &sg, &cg);
+    sincospi_poly(fmaf(c.gpu, u, c.gpv * v), &sg, &cg);
     vre = fmaf(ga, cg, vre);
     vim = fmaf(ga, sg, vim);
   }
   return make_float2(vre, vim);
 }
 
-__global__ void sgra_pack_kernel(const float *coor, const float *dat, const float *std2r,
-                                 const int *icoor, int nvis, int ncph, int cpext,
-                                 float4 *vis, int4 *cli, float4 *clf, int *status);
+// Data packing kernels (defined once, in the library translation unit).
+__global__ void sgra_points_kernel(const float *coor, const float *dat, const float *std2r,
+                                   int nvis, int ncph, int cpext, float4 *raw, float *key);
+__global__ void rank_kernel(const float *key, int n, int *newpos);
+__global__ void sgra_scatter_kernel(const float4 *raw, const float *key, const int *newpos,
+                                    int npts, const int *icoor, const float *dat,
+                                    const float *std2r, int nvis, int ncph, int cpext,
+                                    float4 *vis, float *rho, int *orig, int4 *cli, float4 *clf,
+                                    int *status);
 
 struct SgraModel {
   using Consts = SgraConsts;
   struct Packed {
-    const float4 *vis;   // [npts]: u, v, amp_obs, 1/sigma^2 (0 for triangle points)
-    const int4 *cli;     // [ncph]: point indices i, j, k
-    const float4 *clf;   // [ncph]: cos obs, sin obs, 1/sigma^2, obs
+    const float4 *vis;   // [npts] sorted by |uv|: u, v, amp_obs, 1/sigma^2 (0: triangle point)
+    const float *rho;    // [npts] |uv| of vis
+    const int *orig;     // [npts] index of vis[i] in the caller's order
+    const int4 *cli;     // [ncph] sorted-point indices i, j, k of closure c
+    const float4 *clf;   // [ncph] cos obs, sin obs, 1/sigma^2, obs
     int nvis, npts, ncph, cpext, npass, imodel, phasor, ndat;
   };
 
   static constexpr bool kRowsInEval = false;
+  static constexpr unsigned kTabBytes = sizeof(float2) * kBesselIntervals * (kBesselDeg + 1);
 
+  // shared scratch: Bessel table, then phasors [R][npts] (float2) or phases (float)
   __host__ __device__ static unsigned scratch_bytes(const Packed &pk, int R)
   {
-    return (unsigned)R * (unsigned)pk.npts * (pk.phasor ? 8u : 4u);
+    return kTabBytes + (unsigned)R * (unsigned)pk.npts * (pk.phasor ? 8u : 4u);
   }
 
   // ---- host side: sizes, validation, packing ------------------------------
@@ -146,11 +146,9 @@ struct SgraModel {
         *err = "Sgr A* model: cpExt=1 needs ncoor >= 2*nvis + 4*ncph";
         return CMC_ERR_ARG;
       }
-    } else {
-      if (j.ncoor < 2 * pk.nvis || (pk.npass >= 2 && j.nicoor < 3 * pk.ncph)) {
-        *err = "Sgr A* model: needs ncoor >= 2*nvis and nicoor >= 3*ncph";
-        return CMC_ERR_ARG;
-      }
+    } else if (j.ncoor < 2 * pk.nvis || j.nicoor < 3 * pk.ncph) {
+      *err = "Sgr A* model: needs ncoor >= 2*nvis and nicoor >= 3*ncph";
+      return CMC_ERR_ARG;
     }
     const long long need = (long long)nrep * (j.ndat + pk.nvis);
     if (j.datm != nullptr && j.ndatm < need) {
@@ -163,28 +161,18 @@ struct SgraModel {
 
   static size_t host_work_bytes(const Packed &pk)
   {
-    return (size_t)pk.npts * 16 + (size_t)pk.ncph * 32 + 64;
+    return (size_t)pk.npts * 48 + (size_t)pk.ncph * 32 + 256;
   }
 
-  static int host_pack(const cmc_job &j, Packed &pk, void *work, cudaStream_t s)
-  {
-    unsigned char *w = (unsigned char *)work;
-    size_t o = 0;
-    pk.vis = (const float4 *)(w + o); o += ((size_t)pk.npts * 16 + 15) & ~(size_t)15;
-    pk.cli = (const int4 *)(w + o);   o += (size_t)pk.ncph * 16;
-    pk.clf = (const float4 *)(w + o);
-    const int n = pk.npts + pk.ncph;
-    if (n == 0) return CMC_OK;
-    int blocks = (n + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
-    sgra_pack_kernel<<<blocks, 256, 0, s>>>(j.coor, j.dat, j.std2r, j.icoor, pk.nvis, pk.ncph,
-                                            pk.cpext, (float4 *)pk.vis, (int4 *)pk.cli,
-                                            (float4 *)pk.clf, j.status);
-    return cudaGetLastError() == cudaSuccess ? CMC_OK : CMC_ERR_CUDA;
-  }
+  static int host_pack(const cmc_job &j, Packed &pk, void *work, cudaStream_t s);
 
   template <class Cta>
-  __device__ static void setup(Cta &, int, int) {}
+  __device__ static void setup(Cta &cta, int tid, int T)
+  {
+    float2 *tab = reinterpret_cast<float2 *>(cta.scratch);
+    const float2 *src = &kBesselTab[0][0];
+    for (int i = tid; i < kBesselIntervals * (kBesselDeg + 1); i += T) tab[i] = src[i];
+  }
 
   template <class Cta>
   __device__ static void after_exchange(Cta &) {}
@@ -259,35 +247,30 @@ struct SgraModel {
   {
     const Packed &pk = *cta.pk;
     const int tid = cta.tid, T = cta.nthreads, npts = pk.npts;
+    const float2 *btab = reinterpret_cast<const float2 *>(cta.scratch);
+    float *zs = cta.scratch + kTabBytes / 4;
+    float2 *z = reinterpret_cast<float2 *>(zs);
     bool act[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       acc[r] = 0.0f;
       act[r] = cta.flag[r] != 0;
     }
-    float2 *z = reinterpret_cast<float2 *>(cta.scratch);
-    float *ph = cta.scratch;
     for (int i = tid; i < npts; i += T) {
       const float4 d = __ldg(&pk.vis[i]);
-      const float rho = sqrtf(fmaf(d.x, d.x, d.y * d.y));
+      const float rho = __ldg(&pk.rho[i]);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if (!act[r]) continue;
-        const float2 V = sgra_vis(cta.consts[r], d.x, d.y, rho);
+        const float2 V = sgra_vis(cta.consts[r], btab, d.x, d.y, rho);
         const float n2 = fmaf(V.x, V.x, V.y * V.y);
-        const float amp = sqrtf(n2);
-        const float dif = d.z - amp;
+        const float rs = (n2 > 0.0f) ? rsqrtf(n2) : 0.0f;
+        const float dif = d.z - n2 * rs;
         acc[r] = fmaf(dif * dif, d.w, acc[r]);
-        if (pk.phasor) {
-          float2 zz = make_float2(1.0f, 0.0f);
-          if (n2 > 0.0f) {
-            const float rs = rsqrtf(n2);
-            zz = make_float2(V.x * rs, V.y * rs);
-          }
-          z[r * npts + i] = zz;
-        } else {
-          ph[r * npts + i] = atan2f(V.y, V.x);
-        }
+        if (pk.phasor)
+          z[r * npts + i] = (n2 > 0.0f) ? make_float2(V.x * rs, V.y * rs) : make_float2(1.f, 0.f);
+        else
+          zs[r * npts + i] = atan2_poly(V.y, V.x);
       }
     }
     if (pk.ncph == 0 || pk.npass < 2) return;
@@ -305,9 +288,9 @@ struct SgraModel {
           const float abr = a.x * b.x - a.y * b.y, abi = a.x * b.y + a.y * b.x;
           const float mr = abr * e.x + abi * e.y, mi = abi * e.x - abr * e.y;
           // residual phasor e^{i obs} * conj(m)
-          dif = atan2f(f.y * mr - f.x * mi, f.x * mr + f.y * mi);
+          dif = atan2_poly(f.y * mr - f.x * mi, f.x * mr + f.y * mi);
         } else {
-          const float x = f.w - (ph[r * npts + q.x] + ph[r * npts + q.y] - ph[r * npts + q.z]);
+          const float x = f.w - (zs[r * npts + q.x] + zs[r * npts + q.y] - zs[r * npts + q.z]);
           dif = x - 6.2831853071795865f * rintf(x * 0.15915494309189535f);
         }
         acc[r] = fmaf(dif * dif, f.z, acc[r]);
@@ -322,18 +305,21 @@ struct SgraModel {
   {
     const cmc_job &job = *cta.job;
     const Packed &pk = *cta.pk;
+    const float2 *btab = reinterpret_cast<const float2 *>(cta.scratch);
     const int tid = cta.tid, T = cta.nthreads, nvis = pk.nvis, ndat = pk.ndat;
     const size_t nchi2m = (size_t)job.nbeta * job.nseq * ndat;
-    for (int i = tid; i < nvis; i += T) {
+    for (int i = tid; i < pk.npts; i += T) {
+      const int o = __ldg(&pk.orig[i]);
+      if (o >= nvis) continue;
       const float4 d = __ldg(&pk.vis[i]);
-      const float rho = sqrtf(fmaf(d.x, d.x, d.y * d.y));
+      const float rho = __ldg(&pk.rho[i]);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if (!flags[r]) continue;
         const size_t ist = (size_t)cta.ist[r];
-        const float2 V = sgra_vis(cta.consts[r], d.x, d.y, rho);
-        job.datm[ist * ndat + i] = sqrtf(fmaf(V.x, V.x, V.y * V.y));
-        job.datm[nchi2m + ist * nvis + i] = atan2f(V.y, V.x);
+        const float2 V = sgra_vis(cta.consts[r], btab, d.x, d.y, rho);
+        job.datm[ist * ndat + o] = sqrtf(fmaf(V.x, V.x, V.y * V.y));
+        job.datm[nchi2m + ist * nvis + o] = atan2f(V.y, V.x);
       }
     }
   }
@@ -347,29 +333,31 @@ struct SgraModel {
     const cmc_job &job = *cta.job;
     const Packed &pk = *cta.pk;
     if (job.datm == nullptr || job.chi2m == nullptr) return;
+    const float2 *btab = reinterpret_cast<const float2 *>(cta.scratch);
     const int tid = cta.tid, T = cta.nthreads, npts = pk.npts, nvis = pk.nvis;
     const int ndat = pk.ndat, nptot = job.nptot;
     const size_t nchi2m = (size_t)job.nbeta * job.nseq * ndat;
-    float *ph = cta.scratch;   // phases [R][npts]
+    float *ph = cta.scratch + kTabBytes / 4;   // phases [R][npts]
     __syncthreads();
     if (tid < R && evald[tid]) prepare(cta, tid, plast + tid * nptot);
     __syncthreads();
     for (int i = tid; i < npts; i += T) {
       const float4 d = __ldg(&pk.vis[i]);
-      const float rho = sqrtf(fmaf(d.x, d.x, d.y * d.y));
+      const float rho = __ldg(&pk.rho[i]);
+      const int o = __ldg(&pk.orig[i]);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if (!evald[r]) continue;
-        const float2 V = sgra_vis(cta.consts[r], d.x, d.y, rho);
+        const float2 V = sgra_vis(cta.consts[r], btab, d.x, d.y, rho);
         const float amp = sqrtf(fmaf(V.x, V.x, V.y * V.y));
         const float phase = atan2f(V.y, V.x);
         ph[r * npts + i] = phase;
-        if (i < nvis) {
+        if (o < nvis) {
           const size_t ist = (size_t)cta.ist[r];
           const float dif = d.z - amp;
-          job.datm[ist * ndat + i] = amp;
-          job.datm[nchi2m + ist * nvis + i] = phase;
-          job.chi2m[ist * ndat + i] = (dif * dif) * d.w;
+          job.datm[ist * ndat + o] = amp;
+          job.datm[nchi2m + ist * nvis + o] = phase;
+          job.chi2m[ist * ndat + o] = (dif * dif) * d.w;
         }
       }
     }
@@ -394,27 +382,69 @@ struct SgraModel {
 };
 
 #ifndef CMC_INSTANCE_TU
-// Repack the reference-layout Sgr A* data (coor = [u0,v0,u1,v1,...] plus,
-// for cpExt == 1, [u1,v1,u2,v2] per closure; dat = [amp..., cph...];
-// std2r; icoor triplets) into the fast path's arrays.  Triangle points of
-// cpExt == 1 become extra points with zero amplitude weight.
-__global__ void sgra_pack_kernel(const float *coor, const float *dat, const float *std2r,
-                                 const int *icoor, int nvis, int ncph, int cpext,
-                                 float4 *vis, int4 *cli, float4 *clf, int *status)
+// ---- packing: reference layout -> |uv|-sorted fast-path arrays ------------
+
+// Points in the caller's order: visibilities (coor = [u0,v0,u1,v1,...], dat,
+// std2r) and, for cpExt == 1, the three corners of each closure triangle
+// ([u1,v1,u2,v2] per closure after the visibilities; u3 = -(u1+u2),
+// v3 = -(v1+v2), model.cuh:88-94) with zero amplitude weight.  key = |uv|
+// (NaN -> +inf so that the order stays total).
+__global__ void sgra_points_kernel(const float *coor, const float *dat, const float *std2r,
+                                   int nvis, int ncph, int cpext, float4 *raw, float *key)
 {
   const int npts = nvis + (cpext ? 3 * ncph : 0);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npts + ncph;
-       i += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npts; i += gridDim.x * blockDim.x) {
+    float u, v, a = 0.0f, w = 0.0f;
     if (i < nvis) {
-      vis[i] = make_float4(coor[2 * i], coor[2 * i + 1], dat[i], std2r[i]);
-    } else if (i < npts) {
+      u = coor[2 * i]; v = coor[2 * i + 1]; a = dat[i]; w = std2r[i];
+    } else {
       const int c = (i - nvis) / 3, t = (i - nvis) - 3 * c;
       const int o = 2 * nvis + 4 * c;
-      float u, v;
       if (t == 0) { u = coor[o]; v = coor[o + 1]; }
       else if (t == 1) { u = coor[o + 2]; v = coor[o + 3]; }
       else { u = -(coor[o] + coor[o + 2]); v = -(coor[o + 1] + coor[o + 3]); }
-      vis[i] = make_float4(u, v, 0.0f, 0.0f);
+    }
+    raw[i] = make_float4(u, v, a, w);
+    const float rho = sqrtf(u * u + v * v);
+    key[i] = (rho == rho) ? rho : __int_as_float(0x7f800000);
+  }
+}
+
+// newpos[i] = rank of (key[i], i) in lexicographic order: a deterministic
+// total order, so the packing is identical from run to run.
+__global__ void rank_kernel(const float *key, int n, int *newpos)
+{
+  __shared__ float tile[256];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const float ki = (i < n) ? key[i] : 0.0f;
+  int cnt = 0;
+  for (int base = 0; base < n; base += 256) {
+    const int j = base + threadIdx.x;
+    tile[threadIdx.x] = (j < n) ? key[j] : 0.0f;
+    __syncthreads();
+    const int m = min(256, n - base);
+    for (int t = 0; t < m; ++t) {
+      const float kj = tile[t];
+      cnt += (kj < ki) || (kj == ki && base + t < i);
+    }
+    __syncthreads();
+  }
+  if (i < n) newpos[i] = cnt;
+}
+
+__global__ void sgra_scatter_kernel(const float4 *raw, const float *key, const int *newpos,
+                                    int npts, const int *icoor, const float *dat,
+                                    const float *std2r, int nvis, int ncph, int cpext,
+                                    float4 *vis, float *rho, int *orig, int4 *cli, float4 *clf,
+                                    int *status)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npts + ncph;
+       i += gridDim.x * blockDim.x) {
+    if (i < npts) {
+      const int p = newpos[i];
+      vis[p] = raw[i];
+      rho[p] = key[i];
+      orig[p] = i;
     } else {
       const int c = i - npts;
       int a, b, e;
@@ -430,12 +460,37 @@ __global__ void sgra_pack_kernel(const float *coor, const float *dat, const floa
       const float obs = dat[nvis + c];
       float so, co;
       sincosf(obs, &so, &co);
-      cli[c] = make_int4(a, b, e, 0);
+      cli[c] = make_int4(newpos[a], newpos[b], newpos[e], 0);
       clf[c] = make_float4(co, so, std2r[nvis + c], obs);
     }
   }
 }
 
+int SgraModel::host_pack(const cmc_job &j, Packed &pk, void *work, cudaStream_t s)
+{
+  unsigned char *w = (unsigned char *)work;
+  const size_t n = (size_t)pk.npts, nc = (size_t)pk.ncph;
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  size_t o = 0;
+  float4 *vis = (float4 *)(w + o); o += al(16 * n);
+  float *rho = (float *)(w + o);   o += al(4 * n);
+  int *orig = (int *)(w + o);      o += al(4 * n);
+  int4 *cli = (int4 *)(w + o);     o += al(16 * nc);
+  float4 *clf = (float4 *)(w + o); o += al(16 * nc);
+  float4 *raw = (float4 *)(w + o); o += al(16 * n);
+  float *key = (float *)(w + o);   o += al(4 * n);
+  int *newpos = (int *)(w + o);
+  pk.vis = vis; pk.rho = rho; pk.orig = orig; pk.cli = cli; pk.clf = clf;
+  if (n == 0) return CMC_OK;
+  const int blocks = (int)std::min<size_t>((n + nc + 255) / 256, 4096);
+  sgra_points_kernel<<<blocks, 256, 0, s>>>(j.coor, j.dat, j.std2r, pk.nvis, pk.ncph, pk.cpext,
+                                            raw, key);
+  rank_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(key, (int)n, newpos);
+  sgra_scatter_kernel<<<blocks, 256, 0, s>>>(raw, key, newpos, (int)n, j.icoor, j.dat, j.std2r,
+                                             pk.nvis, pk.ncph, pk.cpext, vis, rho, orig, cli,
+                                             clf, j.status);
+  return cudaGetLastError() == cudaSuccess ? CMC_OK : CMC_ERR_CUDA;
+}
 #endif  // CMC_INSTANCE_TU
 
 }  // namespace cmc
