@@ -23,8 +23,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 MODELS_DIR = os.path.join(PKG, "models")
-LIB_DIR = os.path.join(PKG, "_lib")
-OBJ_DIR = os.path.join(PKG, "_lib", "obj")
+# CMC_LIB_DIR / CMC_NVCC_FLAGS let experiments build variants side by side
+LIB_DIR = os.environ.get("CMC_LIB_DIR", os.path.join(PKG, "_lib"))
+OBJ_DIR = os.path.join(LIB_DIR, "obj")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 R_VALUES = (1, 2, 4, 8, 16, 32)
@@ -39,11 +40,12 @@ def nvcc() -> str:
 
 def _flags():
     return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-            "-I", CSRC, "-I", INCLUDE, "--expt-relaxed-constexpr"]
+            "-I", CSRC, "-I", INCLUDE, "--expt-relaxed-constexpr",
+            *os.environ.get("CMC_NVCC_FLAGS", "").split()]
 
 
 def _sources_digest(extra=()):
-    h = hashlib.sha1()
+    h = hashlib.sha1(os.environ.get("CMC_NVCC_FLAGS", "").encode())
     for d in (CSRC, INCLUDE):
         for name in sorted(os.listdir(d)):
             with open(os.path.join(d, name), "rb") as f:

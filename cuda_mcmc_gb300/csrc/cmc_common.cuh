@@ -94,14 +94,17 @@ struct Rng {
 __host__ __device__ inline unsigned align16(unsigned x) { return (x + 15u) & ~15u; }
 
 // Shared-memory plan of one CTA; the same function sizes the launch on the
-// host and carves the buffer on the device.
+// host and carves the buffer on the device.  `hist` holds the burn-in
+// accept/reject history n_hist as one bit per entry: [R][nprm][hist_words(nadj)].
 struct SmemPlan {
-  unsigned params, plast, ptmp, rf, ri, sf, si, tab, consts, red, xch, stage,
+  unsigned params, plast, ptmp, rf, ri, sf, si, hist, tab, consts, red, xch, stage,
       scratch, total;
 };
 
+__host__ __device__ inline int hist_words(int nadj) { return (nadj + 31) / 32; }
+
 __host__ __device__ inline SmemPlan make_plan(int R, int nthreads, int nptot, int nprm,
-                                              int nbeta, unsigned consts_bytes,
+                                              int nbeta, int nadj, unsigned consts_bytes,
                                               unsigned scratch_bytes)
 {
   SmemPlan p;
@@ -112,7 +115,8 @@ __host__ __device__ inline SmemPlan make_plan(int R, int nthreads, int nptot, in
   p.rf = o;      o = align16(o + 4u * R * kRepF);
   p.ri = o;      o = align16(o + 4u * R * kRepI);
   p.sf = o;      o = align16(o + 4u * R * nprm);
-  p.si = o;      o = align16(o + 4u * R * nprm * 3);
+  p.si = o;      o = align16(o + 4u * R * nprm * 4);
+  p.hist = o;    o = align16(o + 4u * R * nprm * hist_words(nadj));
   p.tab = o;     o = align16(o + 4u * (nprm + 3 * nptot));
   p.consts = o;  o = align16(o + consts_bytes * R);
   p.red = o;     o = align16(o + 4u * R * (nthreads / 32));

@@ -20,7 +20,7 @@ eval_kernel(const cmc_job job, const typename Model::Packed pk, int mode)
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
   const int nptot = job.nptot, nrep = job.nbeta * job.nseq;
-  const SmemPlan P = make_plan(R, T, nptot, 1, 1, sizeof(typename Model::Consts),
+  const SmemPlan P = make_plan(R, T, nptot, 1, 1, 1, sizeof(typename Model::Consts),
                                Model::scratch_bytes(pk, R));
   float *params = (float *)(smem + P.params);
   int *ri = (int *)(smem + P.ri);

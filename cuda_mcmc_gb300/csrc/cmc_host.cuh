@@ -88,9 +88,9 @@ template <class Model>
 size_t plan_bytes(const cmc_job &j, const typename Model::Packed &pk, int R, int T, int sweep)
 {
   if (sweep)
-    return make_plan(R, T, j.nptot, j.nprm, j.nbeta, sizeof(typename Model::Consts),
+    return make_plan(R, T, j.nptot, j.nprm, j.nbeta, j.nadj, sizeof(typename Model::Consts),
                      Model::scratch_bytes(pk, R)).total;
-  return make_plan(R, T, j.nptot, 1, 1, sizeof(typename Model::Consts),
+  return make_plan(R, T, j.nptot, 1, 1, 1, sizeof(typename Model::Consts),
                    Model::scratch_bytes(pk, R)).total;
 }
 
@@ -128,9 +128,12 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         });
         if (n <= 0) continue;
         const int waves = (j.nseq + n - 1) / n;
-        // makespan ~ waves * R; phasors make closures cheaper, and fewer
-        // threads per replica leave less parallelism per proposal
-        const double score = (double)waves * R * (ph ? 1.0 : 1.05) * (T == 64 ? 1.1 : 1.0);
+        // makespan ~ waves * R; measured on GB300 (Sgr A*, 2600 data):
+        // about 32 threads per replica beats 16 or 64, and phases beat
+        // phasors once the phasors cost co-residency
+        const int tpr = T / R;
+        const double shape = (tpr == 32) ? 1.0 : (tpr == 64 || tpr == 16) ? 1.1 : 1.25;
+        const double score = (double)waves * R * (ph ? 1.0 : 1.02) * shape;
         if (score < best - 1e-9) {
           best = score;
           out.R = R; out.G = G; out.T = T; out.phasor = ph; out.smem = smem;

@@ -6,8 +6,14 @@
 
 namespace cmc {
 
+// Minimum resident CTAs per SM the register allocation is sized for
+// (ptxas: 65536 / (kMaxThreads * CMC_MIN_BLOCKS) registers per thread).
+#ifndef CMC_MIN_BLOCKS
+#define CMC_MIN_BLOCKS 2
+#endif
+
 template <class Model, int R>
-__global__ void __launch_bounds__(kMaxThreads)
+__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
 sweep_kernel(const cmc_job job, const typename Model::Packed pk)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -19,7 +25,7 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
   const int nbeta = job.nbeta, nseq = job.nseq, nptot = job.nptot, nprm = job.nprm;
   const int nadj = job.nadj;
 
-  const SmemPlan P = make_plan(R, T, nptot, nprm, nbeta, sizeof(typename Model::Consts),
+  const SmemPlan P = make_plan(R, T, nptot, nprm, nbeta, nadj, sizeof(typename Model::Consts),
                                Model::scratch_bytes(pk, R));
   float *params = (float *)(smem + P.params);   // [R][nptot]
   float *plast = (float *)(smem + P.plast);     // [R][nptot] params of last evaluation
@@ -31,7 +37,10 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
   float *s_pstp = (float *)(smem + P.sf);       // [R][nprm]
   int *s_ncnt = (int *)(smem + P.si);           // [R][nprm]
   int *s_nacpt = s_ncnt + R * nprm;
-  int *s_hsum = s_nacpt + R * nprm;
+  int *s_hsum = s_nacpt + R * nprm;             // running sum of the history ring
+  int *s_hslow = s_hsum + R * nprm;             // 1: ring holds values other than 0/1
+  unsigned *s_hbits = (unsigned *)(smem + P.hist);   // [R][nprm][HW] history bits
+  const int HW = hist_words(nadj);
   int *s_ivar = (int *)(smem + P.tab);
   int *s_pdescr = s_ivar + nprm;
   float *s_pmin = (float *)(s_pdescr + nptot);
@@ -78,10 +87,21 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
     s_pstp[i] = job.pstp[gi];
     s_ncnt[i] = job.n_cnt[gi];
     s_nacpt[i] = job.n_acpt[gi];
-    int h = 0;
-    for (int a = 0; a < nadj; ++a)
-      h += job.n_hist[(((size_t)nprm * a + k) * nbeta + ibeta) * nseq + iseq];
+    // n_hist[a][k][ibeta][iseq] for a = 0..nadj-1 -> one bit each; a ring
+    // holding other values than 0/1 keeps using the global array
+    int h = 0, slow = 0;
+    for (int w = 0; w < HW; ++w) {
+      unsigned bits = 0u;
+      for (int b = 0; b < 32 && 32 * w + b < nadj; ++b) {
+        const int v = job.n_hist[(((size_t)nprm * (32 * w + b) + k) * nbeta + ibeta) * nseq + iseq];
+        h += v;
+        slow |= (v != 0 && v != 1);
+        bits |= (v != 0 ? 1u : 0u) << b;
+      }
+      s_hbits[i * HW + w] = bits;
+    }
     s_hsum[i] = h;
+    s_hslow[i] = slow;
   }
   if (rank == 0) {
     for (int s = tid; s < nbeta; s += T) {
@@ -150,13 +170,61 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
     __syncthreads();
   }
 
+  // spmp_mcmc (src/gpu_mcmc.cu:426-474) and, in burn-in, adjust_steps
+  // (:480-526) for local replica r, after its proposal has been evaluated.
+  // Runs on thread r, fused with that thread's next proposal so that one
+  // barrier per proposal disappears.
+  auto accept_adjust = [&](int r, bool burn) {
+    const int ibeta = rank * R + r;
+    const int k = s_k[r];
+    if (s_flag[r] != 0) {
+      float c2 = 0.f;
+      for (int w = 0; w < NW; ++w) c2 += s_red[r * NW + w];
+      s_chi2n[r] = c2;
+      const float a = expf(-0.5f * s_beta[r] * (c2 - s_chi2c[r]));
+      const float alpha = (a < 1.0f) ? a : 1.0f;
+      const float u = rng.uniform();
+      if (u <= alpha) {
+        s_chi2c[r] = c2;
+        s_nacpt[r * nprm + k] += 1;
+      } else {
+        params[r * nptot + s_ptentn[r]] = s_ptent[r];
+        s_flag[r] = 0;
+      }
+    }
+    if (burn) {
+      const int ik = r * nprm + k;
+      const int cnt = s_ncnt[ik];
+      int modn = cnt % nadj;
+      if (modn < 0) modn += nadj;   // guards a negative n_cnt from the caller
+      const int nw = (s_flag[r] != 0) ? 1 : 0;
+      if (s_hslow[ik]) {
+        int *hp = &job.n_hist[(((size_t)nprm * modn + k) * nbeta + ibeta) * nseq + iseq];
+        s_hsum[ik] += nw - *hp;
+        *hp = nw;
+      } else {
+        unsigned &word = s_hbits[ik * HW + (modn >> 5)];
+        const unsigned bit = 1u << (modn & 31);
+        s_hsum[ik] += nw - ((word & bit) ? 1 : 0);
+        word = nw ? (word | bit) : (word & ~bit);
+      }
+      const float rate = (float)s_hsum[ik] / (float)((nadj < cnt) ? nadj : cnt);
+      if (rate < 0.30f)
+        s_pstp[ik] = (float)((double)s_pstp[ik] / 1.01);
+      else
+        s_pstp[ik] = (float)((double)s_pstp[ik] * 1.01);
+      s_ncnt[ik] = cnt + 1;
+    }
+  };
+
   const int nsteps = job.nburn + job.niter;
   for (int step = 0; step < nsteps; ++step) {
     const bool burn = step < job.nburn;
     for (int ipm = 0; ipm < nprm; ++ipm) {
-      // gen_proposal (src/gpu_mcmc.cu:361-411)
       if (tid < R) {
         const int r = tid;
+        if (ipm > 0) accept_adjust(r, burn);
+        // gen_proposal (src/gpu_mcmc.cu:361-411)
         const int k = rng.index(nprm, job.status);
         const int t = s_ivar[k];
         float p = params[r * nptot + t];
@@ -183,44 +251,8 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
       Model::template eval<R>(cta, acc);
       block_reduce<Model, R>(acc, s_red, tid, NW);
       __syncthreads();
-      // spmp_mcmc (src/gpu_mcmc.cu:426-474) and adjust_steps (:480-526)
-      if (tid < R) {
-        const int r = tid, ibeta = rank * R + r;
-        const int k = s_k[r];
-        if (s_flag[r] != 0) {
-          float c2 = 0.f;
-          for (int w = 0; w < NW; ++w) c2 += s_red[r * NW + w];
-          s_chi2n[r] = c2;
-          const float a = expf(-0.5f * s_beta[r] * (c2 - s_chi2c[r]));
-          const float alpha = (a < 1.0f) ? a : 1.0f;
-          const float u = rng.uniform();
-          if (u <= alpha) {
-            s_chi2c[r] = c2;
-            s_nacpt[r * nprm + k] += 1;
-          } else {
-            params[r * nptot + s_ptentn[r]] = s_ptent[r];
-            s_flag[r] = 0;
-          }
-        }
-        if (burn) {
-          const int ik = r * nprm + k;
-          const int cnt = s_ncnt[ik];
-          int modn = cnt % nadj;
-          if (modn < 0) modn += nadj;   // guards a negative n_cnt from the caller
-          int *hp = &job.n_hist[(((size_t)nprm * modn + k) * nbeta + ibeta) * nseq + iseq];
-          const int nw = (s_flag[r] != 0) ? 1 : 0;
-          s_hsum[ik] += nw - *hp;
-          *hp = nw;
-          const float rate = (float)s_hsum[ik] / (float)((nadj < cnt) ? nadj : cnt);
-          if (rate < 0.30f)
-            s_pstp[ik] = (float)((double)s_pstp[ik] / 1.01);
-          else
-            s_pstp[ik] = (float)((double)s_pstp[ik] * 1.01);
-          s_ncnt[ik] = cnt + 1;
-        }
-      }
-      __syncthreads();
     }
+    if (tid < R) accept_adjust(tid, burn);
 
     // ---- replica_exchange (src/gpu_mcmc.cu:533-626) ------------------------
     cluster.sync();
@@ -309,6 +341,11 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
     job.pstp[gi] = s_pstp[i];
     job.n_cnt[gi] = s_ncnt[i];
     job.n_acpt[gi] = s_nacpt[i];
+    if (!s_hslow[i] && job.nburn > 0) {
+      for (int a = 0; a < nadj; ++a)
+        job.n_hist[(((size_t)nprm * a + k) * nbeta + ibeta) * nseq + iseq] =
+            (s_hbits[i * HW + (a >> 5)] >> (a & 31)) & 1u;
+    }
   }
   if (rank == 0) {
     for (int s = tid; s < nbeta; s += T) {

@@ -29,6 +29,30 @@ __device__ __forceinline__ void sincospi_poly(float t, float *s, float *c)
   *c = sg * pc;
 }
 
+// sin(pi t), cos(pi t) from the hardware approximations: t is reduced to
+// r = t - rint(t) in [-1/2, 1/2] first, where __sinf / __cosf have an
+// absolute error below 2^-21.4.
+__device__ __forceinline__ void sincospi_mufu(float t, float *s, float *c)
+{
+  const float n = rintf(t);
+  const float x = (t - n) * 3.14159265358979324f;
+  const float sg = (((int)n) & 1) ? -1.0f : 1.0f;
+  *s = sg * __sinf(x);
+  *c = sg * __cosf(x);
+}
+
+#ifndef CMC_MUFU_SINCOS
+#define CMC_MUFU_SINCOS 1
+#endif
+__device__ __forceinline__ void sincospi_fast(float t, float *s, float *c)
+{
+#if CMC_MUFU_SINCOS
+  sincospi_mufu(t, s, c);
+#else
+  sincospi_poly(t, s, c);
+#endif
+}
+
 // atan2(y, x) in [-pi, pi]: a = min/max of |x|, |y| in [0, 1], atan(a) from
 // the polynomial, then the octant.  atan2(0, 0) = 0.
 __device__ __forceinline__ float atan2_poly(float y, float x)
@@ -47,26 +71,29 @@ __device__ __forceinline__ float atan2_poly(float y, float x)
 }
 
 // F1(x) = J1(x)/x and F2(x) = J2(x)/x^2 (even in x) from the piecewise
-// polynomial table `tab` (a shared-memory copy of kBesselTab); beyond the
-// table, from CUDA's j0f/j1f with J2 = 2 J1/x - J0.
-__device__ __forceinline__ void bessel_f12_tab(const float2 *tab, float x, float &f1, float &f2)
+// polynomial table `tab` (a shared-memory copy of kBesselTab: per interval,
+// (kBesselDeg + 1) / 2 float4 of coefficient pairs).  BIG = false: x is known
+// to lie inside the table (straight-line code); BIG = true: beyond the table
+// F1, F2 come from CUDA's j0f/j1f with J2 = 2 J1/x - J0.
+template <bool BIG>
+__device__ __forceinline__ void bessel_f12_tab(const float4 *tab, float x, float &f1, float &f2)
 {
+  constexpr int kQ = (kBesselDeg + 1) / 2;
   x = fabsf(x);
-  if (x < (float)kBesselIntervals) {
-    const int i = (int)x;
-    const float d = x - ((float)i + 0.5f);
-    const float2 *c = tab + i * (kBesselDeg + 1);
-    float2 a = c[kBesselDeg];
-    float p1 = a.x, p2 = a.y;
+  const int i = min((int)x, kBesselIntervals - 1);
+  const float d = x - ((float)i + 0.5f);
+  const float4 *c = tab + i * kQ;
+  float4 a = c[kQ - 1];
+  float p1 = fmaf(a.z, d, a.x), p2 = fmaf(a.w, d, a.y);
 #pragma unroll
-    for (int k = kBesselDeg - 1; k >= 0; --k) {
-      a = c[k];
-      p1 = fmaf(p1, d, a.x);
-      p2 = fmaf(p2, d, a.y);
-    }
-    f1 = p1;
-    f2 = p2;
-  } else {
+  for (int m = kQ - 2; m >= 0; --m) {
+    a = c[m];
+    p1 = fmaf(fmaf(p1, d, a.z), d, a.x);
+    p2 = fmaf(fmaf(p2, d, a.w), d, a.y);
+  }
+  f1 = p1;
+  f2 = p2;
+  if (BIG && x >= (float)kBesselIntervals) {
     const float ix = 1.0f / x;
     const float j0 = j0f(x), j1 = j1f(x);
     f1 = j1 * ix;

@@ -20,8 +20,8 @@ from numpy.polynomial import chebyshev as Ch
 from numpy.polynomial import polynomial as Po
 from scipy.special import j1, jv
 
-XMAX = 16
-DEG = 9
+XMAX = 32
+DEG = 9            # odd: coefficients pack into (DEG + 1) / 2 float4
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -80,17 +80,20 @@ def main():
         "//",
         "// F1(x) = J1(x)/x and F2(x) = J2(x)/x^2 on [0, %d): interval i = [i, i+1) holds" % XMAX,
         "// coefficients a_k (k = 0..%d) of sum_k a_k d^k, d = x - (i + 0.5), stored as" % DEG,
-        "// pairs (F1 a_k, F2 a_k).  Chebyshev interpolants of float64 values, rounded",
+        "// float4 (F1 a_2m, F2 a_2m, F1 a_2m+1, F2 a_2m+1), m = 0..%d.  Chebyshev" % ((DEG - 1) // 2),
+        "// interpolants of float64 values, rounded",
         "// to float32; max |error| with float32 Horner: F1 %.2e, F2 %.2e." % tuple(err),
         "#pragma once",
         "",
         "namespace cmc {",
         "constexpr int kBesselIntervals = %d;" % XMAX,
         "constexpr int kBesselDeg = %d;" % DEG,
-        "static __device__ const float2 kBesselTab[%d][%d] = {" % (XMAX, DEG + 1),
+        "static __device__ const float4 kBesselTab[%d][%d] = {" % (XMAX, (DEG + 1) // 2),
     ]
     for i in range(XMAX):
-        row = ", ".join("{%.9ef, %.9ef}" % (tab[i, k, 0], tab[i, k, 1]) for k in range(DEG + 1))
+        row = ", ".join("{%.9ef, %.9ef, %.9ef, %.9ef}" % (tab[i, 2 * m, 0], tab[i, 2 * m, 1],
+                                                           tab[i, 2 * m + 1, 0], tab[i, 2 * m + 1, 1])
+                        for m in range((DEG + 1) // 2))
         lines.append("    {%s}," % row)
     lines += ["};", "}  // namespace cmc", ""]
     with open(os.path.join(HERE, "bessel_table.cuh"), "w") as f:

@@ -51,37 +51,33 @@ struct SgraConsts {
   float gpu, gpv;   // Gaussian phase / pi = gpu u + gpv v
   float zr, zg;     // ring and Gaussian weights
   int inner, gauss, ring;
+  int bigx;         // some Bessel argument of this replica is beyond the table
 };
 
 // Model visibility V = Vre + i Vim of one replica at (u, v), |uv| = rho.
-__device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, const float2 *btab, float u,
+// Straight-line code: a switched-off component (no inner disk: ai = bi = 0;
+// no Gaussian: zg = 0; sgra_model13 Gaussian-only: ring = 0) contributes
+// zero, so the evaluations of different replicas can be interleaved.
+template <bool BIG = true>
+__device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, const float4 *btab, float u,
                                           float v, float rho)
 {
-  float vre = 0.0f, vim = 0.0f;
-  if (c.ring) {
-    const float U = fmaf(u, c.cth, v * c.sth);
-    float f1, f2;
-    bessel_f12_tab(btab, c.kex * rho, f1, f2);
-    float re = c.ae * f1, im = c.be * f2 * U;
-    if (c.inner) {
-      float g1, g2, sd, cd;
-      bessel_f12_tab(btab, c.kin * rho, g1, g2);
-      const float rei = c.ai * g1, imi = c.bi * g2 * U;
-      sincospi_poly(c.dsh * U, &sd, &cd);
-      re -= rei * cd - imi * sd;
-      im -= rei * sd + imi * cd;
-    }
-    vre = c.zr * re;
-    vim = c.zr * im;
-  }
-  if (c.gauss) {
-    const float ug = fmaf(u, c.gc, v * c.gs), vg = fmaf(v, c.gc, -u * c.gs);
-    const float ga = c.zg * __expf(-fmaf(c.gx * ug, ug, c.gy * vg * vg));
-    float sg, cg;
-    sincospi_poly(fmaf(c.gpu, u, c.gpv * v), &sg, &cg);
-    vre = fmaf(ga, cg, vre);
-    vim = fmaf(ga, sg, vim);
-  }
+  const float U = fmaf(u, c.cth, v * c.sth);
+  float f1, f2, g1, g2, sd, cd;
+  bessel_f12_tab<BIG>(btab, c.kex * rho, f1, f2);
+  bessel_f12_tab<BIG>(btab, c.kin * rho, g1, g2);
+  sincospi_fast(c.dsh * U, &sd, &cd);
+  const float rei = c.ai * g1, imi = c.bi * g2 * U;
+  const float re = c.ae * f1 - (rei * cd - imi * sd);
+  const float im = c.be * f2 * U - (rei * sd + imi * cd);
+  float vre = c.ring ? c.zr * re : 0.0f;
+  float vim = c.ring ? c.zr * im : 0.0f;
+  const float ug = fmaf(u, c.gc, v * c.gs), vg = fmaf(v, c.gc, -u * c.gs);
+  const float ga = c.zg * __expf(-fmaf(c.gx * ug, ug, c.gy * vg * vg));
+  float sg, cg;
+  sincospi_fast(fmaf(c.gpu, u, c.gpv * v), &sg, &cg);
+  vre = fmaf(ga, cg, vre);
+  vim = fmaf(ga, sg, vim);
   return make_float2(vre, vim);
 }
 
@@ -95,6 +91,12 @@ __global__ void sgra_scatter_kernel(const float4 *raw, const float *key, const i
                                     float4 *vis, float *rho, int *orig, int4 *cli, float4 *clf,
                                     int *status);
 
+// CMC_BRANCHFREE: evaluate every local replica and drop the terms of the
+// inactive ones, so that the R independent evaluations interleave.
+#ifndef CMC_BRANCHFREE
+#define CMC_BRANCHFREE 1
+#endif
+
 struct SgraModel {
   using Consts = SgraConsts;
   struct Packed {
@@ -107,7 +109,8 @@ struct SgraModel {
   };
 
   static constexpr bool kRowsInEval = false;
-  static constexpr unsigned kTabBytes = sizeof(float2) * kBesselIntervals * (kBesselDeg + 1);
+  static constexpr unsigned kTabBytes =
+      (unsigned)sizeof(float4) * kBesselIntervals * ((kBesselDeg + 1) / 2);
 
   // shared scratch: Bessel table, then phasors [R][npts] (float2) or phases (float)
   __host__ __device__ static unsigned scratch_bytes(const Packed &pk, int R)
@@ -169,9 +172,9 @@ struct SgraModel {
   template <class Cta>
   __device__ static void setup(Cta &cta, int tid, int T)
   {
-    float2 *tab = reinterpret_cast<float2 *>(cta.scratch);
-    const float2 *src = &kBesselTab[0][0];
-    for (int i = tid; i < kBesselIntervals * (kBesselDeg + 1); i += T) tab[i] = src[i];
+    float4 *tab = reinterpret_cast<float4 *>(cta.scratch);
+    const float4 *src = &kBesselTab[0][0];
+    for (int i = tid; i < (int)(kTabBytes / sizeof(float4)); i += T) tab[i] = src[i];
   }
 
   template <class Cta>
@@ -204,8 +207,8 @@ struct SgraModel {
     c.ae = 0.5f * (h + h0) * Rex * c.kex;
     c.be = -(h - h0) / (4.0f * pi) * (c.kex * c.kex * c.kex);
     c.inner = (Rin != 0.0f);
-    c.ai = 0.5f * (h + h0 - d * (h - h0) / Rex) * Rin * c.kin;
-    c.bi = -(h - h0) / (4.0f * pi) * rq * (c.kin * c.kin * c.kin);
+    c.ai = c.inner ? 0.5f * (h + h0 - d * (h - h0) / Rex) * Rin * c.kin : 0.0f;
+    c.bi = c.inner ? -(h - h0) / (4.0f * pi) * rq * (c.kin * c.kin * c.kin) : 0.0f;
     c.dsh = 2.0f * d;
     // 2 (pi / (2 sqrt(2 ln 2)))^2 = pi^2 / (4 ln 2): FWHM^2 -> Gaussian exponent
     const float gcoef = 3.5597039f;
@@ -239,15 +242,35 @@ struct SgraModel {
       c.zg = Zsp;
       c.gauss = !(gax == 0.0f || aq == 0.0f);
     }
+    if (!c.gauss) c.zg = 0.0f;
+    const float rho_max = (cta.pk->npts > 0) ? cta.pk->rho[cta.pk->npts - 1] : 0.0f;
+    c.bigx = !(fmaxf(fabsf(c.kex), fabsf(c.kin)) * rho_max < (float)kBesselIntervals);
   }
 
-  // chi^2 of every active replica over all data (both passes).
+  // chi^2 of every active replica over all data (both passes).  The phase
+  // storage mode and the need for the out-of-table Bessel path are uniform
+  // over the CTA: each combination is its own straight-line loop.
   template <int R, class Cta>
   __device__ static void eval(Cta &cta, float (&acc)[R])
   {
+    bool big = false;
+#pragma unroll
+    for (int r = 0; r < R; ++r) big |= (cta.flag[r] != 0 && cta.consts[r].bigx != 0);
+    if (cta.pk->phasor) {
+      if (big) eval_impl<R, true, true>(cta, acc);
+      else eval_impl<R, true, false>(cta, acc);
+    } else {
+      if (big) eval_impl<R, false, true>(cta, acc);
+      else eval_impl<R, false, false>(cta, acc);
+    }
+  }
+
+  template <int R, bool PH, bool BIG, class Cta>
+  __device__ static void eval_impl(Cta &cta, float (&acc)[R])
+  {
     const Packed &pk = *cta.pk;
     const int tid = cta.tid, T = cta.nthreads, npts = pk.npts;
-    const float2 *btab = reinterpret_cast<const float2 *>(cta.scratch);
+    const float4 *btab = reinterpret_cast<const float4 *>(cta.scratch);
     float *zs = cta.scratch + kTabBytes / 4;
     float2 *z = reinterpret_cast<float2 *>(zs);
     bool act[R];
@@ -261,13 +284,15 @@ struct SgraModel {
       const float rho = __ldg(&pk.rho[i]);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
+#if !CMC_BRANCHFREE
         if (!act[r]) continue;
-        const float2 V = sgra_vis(cta.consts[r], btab, d.x, d.y, rho);
+#endif
+        const float2 V = sgra_vis<BIG>(cta.consts[r], btab, d.x, d.y, rho);
         const float n2 = fmaf(V.x, V.x, V.y * V.y);
         const float rs = (n2 > 0.0f) ? rsqrtf(n2) : 0.0f;
         const float dif = d.z - n2 * rs;
-        acc[r] = fmaf(dif * dif, d.w, acc[r]);
-        if (pk.phasor)
+        acc[r] = fmaf(act[r] ? dif * dif : 0.0f, d.w, acc[r]);
+        if (PH)
           z[r * npts + i] = (n2 > 0.0f) ? make_float2(V.x * rs, V.y * rs) : make_float2(1.f, 0.f);
         else
           zs[r * npts + i] = atan2_poly(V.y, V.x);
@@ -280,9 +305,11 @@ struct SgraModel {
       const float4 f = __ldg(&pk.clf[c]);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
+#if !CMC_BRANCHFREE
         if (!act[r]) continue;
+#endif
         float dif;
-        if (pk.phasor) {
+        if (PH) {
           const float2 a = z[r * npts + q.x], b = z[r * npts + q.y], e = z[r * npts + q.z];
           // m = a * b * conj(e): model closure phasor
           const float abr = a.x * b.x - a.y * b.y, abi = a.x * b.y + a.y * b.x;
@@ -293,7 +320,7 @@ struct SgraModel {
           const float x = f.w - (zs[r * npts + q.x] + zs[r * npts + q.y] - zs[r * npts + q.z]);
           dif = x - 6.2831853071795865f * rintf(x * 0.15915494309189535f);
         }
-        acc[r] = fmaf(dif * dif, f.z, acc[r]);
+        acc[r] = fmaf(act[r] ? dif * dif : 0.0f, f.z, acc[r]);
       }
     }
   }
@@ -305,7 +332,7 @@ struct SgraModel {
   {
     const cmc_job &job = *cta.job;
     const Packed &pk = *cta.pk;
-    const float2 *btab = reinterpret_cast<const float2 *>(cta.scratch);
+    const float4 *btab = reinterpret_cast<const float4 *>(cta.scratch);
     const int tid = cta.tid, T = cta.nthreads, nvis = pk.nvis, ndat = pk.ndat;
     const size_t nchi2m = (size_t)job.nbeta * job.nseq * ndat;
     for (int i = tid; i < pk.npts; i += T) {
@@ -333,7 +360,7 @@ struct SgraModel {
     const cmc_job &job = *cta.job;
     const Packed &pk = *cta.pk;
     if (job.datm == nullptr || job.chi2m == nullptr) return;
-    const float2 *btab = reinterpret_cast<const float2 *>(cta.scratch);
+    const float4 *btab = reinterpret_cast<const float4 *>(cta.scratch);
     const int tid = cta.tid, T = cta.nthreads, npts = pk.npts, nvis = pk.nvis;
     const int ndat = pk.ndat, nptot = job.nptot;
     const size_t nchi2m = (size_t)job.nbeta * job.nseq * ndat;
