@@ -97,6 +97,17 @@ int cmc_reset_gpu(void);
  * the kernels report device-side failures in job->status. */
 int cmc_run(const cmc_job *job, void *stream);
 
+/* libcmc_sgra.so only.  No counterpart in the reference.  cmc_run for callers
+ * that cannot allocate device memory at run time (their memory is reserved
+ * up front by another allocator, or a cudaMalloc / cudaFree would synchronise
+ * a latency-critical pipeline): job->work is ignored and the packed-data
+ * scratch comes from a fixed 4 MiB array inside the library instead (about
+ * 80,000 points; larger jobs are rejected with CMC_ERR_ARG).  The array's
+ * address is resolved by the first call on each device, which should come
+ * before any stream capture; all calls share the array, so calls that
+ * overlap on the GPU race. */
+int cmc_run_noalloc(const cmc_job *job, void *stream);
+
 /* Reference counterpart: run_calcmodchi2 / run_calcmodel
  * (src/gpu_mcmc.cu:769-802) on device arrays: mode 1 = calc_modchi2,
  * mode 2 = calc_model.  Asynchronous on `stream`. */
