@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--nbeta", type=int, default=32)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="use the library's heuristic shape")
+    ap.add_argument("--workload", default="sgra", choices=["sgra", "batch"],
+                    help="sgra: one 64x32 Sgr A* fit; batch: many independent fits")
+    ap.add_argument("--nfits", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -311,6 +315,8 @@ def run_mine(args, rank, world, local):
     _lib.load("sgra")
     w = workload(args, rank)
     job = DeviceJob.from_workload(w, niter_total=args.main_per_step, seed=1234 + rank)
+    if not args.no_tune:
+        job.autotune()
     cfg = job.config()
     stream = torch.cuda.current_stream()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -382,10 +388,80 @@ def run_mine(args, rank, world, local):
     print(json.dumps(line))
 
 
+def run_batch(args, rank, world, local):
+    """Many independent Sgr A* fits (nvis ~ logU(500, 50000), ncph = 0.3 nvis,
+    16 x 16 replicas each): persistent work-list launches replayed from a CUDA
+    graph, against a loop of one plain cmc_run launch per fit."""
+    import torch
+    from cuda_mcmc_gb300 import synth
+    from cuda_mcmc_gb300.device import BatchJob, DeviceJob
+    nb, ni = 1, 3
+    fits = synth.sgra_batch(nfits=args.nfits, seed=5 + rank, nseq=16, nbeta=16, nburn=nb,
+                            niter=ni)
+    jobs = [DeviceJob.from_workload(w, niter_total=ni, seed=77 + i) for i, w in enumerate(fits)]
+    batch = BatchJob(jobs)
+    batch.run(0, 0, do_init=True)
+    batch.check()
+    g = batch.graph(nb, ni, itr0=0)
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    terms = sum(w.nvis + (w.ndat - w.nvis) for w in fits)
+    evals = (nb + ni) * sum(w.nprm * w.nbeta * w.nseq for w in fits)
+    with Clocks(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            g.replay()
+        torch.cuda.synchronize()
+        barrier(world)
+        dt = time.perf_counter() - t0
+    batch.check()
+    dt = max_over_ranks(dt, world)
+    value = evals * args.steps * world / dt
+    # plain: one cmc_run per fit per chunk, heuristic shape, no graph
+    for j in jobs[: min(8, len(jobs))]:
+        j.run(nb, ni, itr0=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for j in jobs:
+        j.run(nb, ni, itr0=0)
+    torch.cuda.synchronize()
+    plain_dt = time.perf_counter() - t0
+    if rank != 0:
+        return
+    fl = sum(w.nprm * w.nbeta * w.nseq * (w.nvis * FLOP_PER_AMP + (w.ndat - w.nvis) * FLOP_PER_CPH)
+             for w in fits) * (nb + ni)
+    peak = fp32_peak_tflops()
+    line = {
+        "metric": "chi2 model evals/sec", "value": value, "unit": "chi2 evals/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "%d independent sgra9 fits, nvis logU(500,50000), ncph 0.3 nvis, "
+                               "16x16 replicas each (%d data in total)" % (len(fits), terms),
+                   "step": "%d burn-in + %d main iterations of every fit" % (nb, ni),
+                   "parallelism": "replicas only", "classes": batch.classes(),
+                   "l2": "inputs larger than L2 in total"},
+        "roofline": {"bound": "fp32", "achieved": fl * args.steps / dt / 1e12, "peak": peak,
+                     "unit": "TFLOP/s", "frac": fl * args.steps / dt / 1e12 / peak,
+                     "traffic": None, "peak_source": "measured cuBLAS SGEMM (TF32 off)"},
+        "plain_per_fit_loop": {"value": evals / plain_dt, "unit": "chi2 evals/s",
+                               "s_per_step": plain_dt},
+        "per_fit_s_per_iteration": dt / args.steps / (nb + ni) / len(fits),
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * len(batch.classes()),
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args)
-    if args.impl == "reference":
+    if args.impl == "mine" and args.workload == "batch":
+        run_batch(args, rank, world, local)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_mine(args, rank, world, local)

@@ -28,7 +28,9 @@ LIB_DIR = os.environ.get("CMC_LIB_DIR", os.path.join(PKG, "_lib"))
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-R_VALUES = (1, 2, 4, 8, 16, 32)
+# replicas-per-CTA instances per library (must match each model's kMaxR)
+R_VALUES = {"sgra": (1, 2, 4, 8)}
+R_VALUES_PLUGIN = (1, 2, 4, 8, 16, 32)
 BUILTIN_PLUGINS = ("rosenbrock", "solvsys", "nlsys")
 
 
@@ -73,7 +75,7 @@ def _jobs_for(name, plugin_file=None):
         abi_src, inst_src = os.path.join(CSRC, "lib_%s.cu" % name), os.path.join(CSRC, "inst_%s.cu" % name)
     o = os.path.join(OBJ_DIR, "%s_abi.o" % name)
     jobs.append((o, [nvcc(), *_flags(), *defs, "-c", abi_src, "-o", o]))
-    for r in R_VALUES:
+    for r in (R_VALUES_PLUGIN if plugin_file is not None else R_VALUES[name]):
         o = os.path.join(OBJ_DIR, "%s_r%d.o" % (name, r))
         jobs.append((o, [nvcc(), *_flags(), *defs, "-DCMC_R=%d" % r, "-c", inst_src, "-o", o]))
     return jobs

@@ -68,7 +68,8 @@ CALC_MODEL_ARGS = [_fp, _ip, _fp, _fp] + [C.c_int] * 8
 EXPORTS = ("mcmc_cuda", "mcmc_cuda_v2", "calc_modchi2", "calc_modchi2_v2", "calc_model",
            "calc_model_v2", "cmc_last_error", "cmc_model_name", "cmc_abi_version",
            "cmc_sizeof_job", "cmc_reset_gpu", "cmc_work_bytes", "cmc_run", "cmc_eval",
-           "cmc_query_config", "cmc_set_config")
+           "cmc_query_config", "cmc_set_config", "cmc_batch_work_bytes", "cmc_batch_prepare",
+           "cmc_batch_run", "cmc_batch_info", "cmc_batch_free")
 
 
 def _declare(L):
@@ -100,6 +101,18 @@ def _declare(L):
     L.cmc_query_config.restype = C.c_int
     L.cmc_set_config.argtypes = [C.c_int, C.c_int, C.c_int]
     L.cmc_set_config.restype = None
+    L.cmc_batch_work_bytes.argtypes = [C.POINTER(CmcJob), C.c_int]
+    L.cmc_batch_work_bytes.restype = C.c_size_t
+    L.cmc_batch_prepare.argtypes = [C.POINTER(CmcJob), C.c_int, C.c_void_p, C.c_size_t,
+                                    C.c_void_p]
+    L.cmc_batch_prepare.restype = C.c_void_p
+    L.cmc_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    L.cmc_batch_run.restype = C.c_int
+    L.cmc_batch_info.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _ip, _ip,
+                                 C.POINTER(C.c_size_t)]
+    L.cmc_batch_info.restype = C.c_int
+    L.cmc_batch_free.argtypes = [C.c_void_p]
+    L.cmc_batch_free.restype = None
     if L.cmc_sizeof_job() != C.sizeof(CmcJob):
         raise RuntimeError("cmc_job layout mismatch between %s and _lib.CmcJob" % L._name)
 

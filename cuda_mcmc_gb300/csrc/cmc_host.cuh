@@ -14,6 +14,7 @@
 #include <cstring>
 #include <string>
 #include <type_traits>
+#include <vector>
 
 #include "cmc_common.cuh"
 #include "cmc_job.h"
@@ -62,7 +63,9 @@ inline int env_int(const char *name, int dflt)
   return (v && *v) ? std::atoi(v) : dflt;
 }
 
-template <class F>
+// Calls f(std::integral_constant<int, R>) for the instantiated R values of
+// the model (R <= Model::kMaxR).
+template <class Model, class F>
 inline int dispatch_R(int R, F &&f)
 {
   switch (R) {
@@ -70,10 +73,15 @@ inline int dispatch_R(int R, F &&f)
     case 2: return f(std::integral_constant<int, 2>{});
     case 4: return f(std::integral_constant<int, 4>{});
     case 8: return f(std::integral_constant<int, 8>{});
-    case 16: return f(std::integral_constant<int, 16>{});
-    case 32: return f(std::integral_constant<int, 32>{});
-    default: return fail(CMC_ERR_UNSUPPORTED, "no kernel instance for this replicas-per-CTA count");
+    case 16:
+      if constexpr (Model::kMaxR >= 16) return f(std::integral_constant<int, 16>{});
+      break;
+    case 32:
+      if constexpr (Model::kMaxR >= 32) return f(std::integral_constant<int, 32>{});
+      break;
+    default: break;
   }
+  return fail(CMC_ERR_UNSUPPORTED, "no kernel instance for this replicas-per-CTA count");
 }
 
 inline int smem_optin()
@@ -109,6 +117,7 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
   bool found = false;
   const int Rs[] = {1, 2, 4, 8, 16, 32};
   for (int R : Rs) {
+    if (R > Model::kMaxR) continue;
     if (Rfix && R != Rfix) continue;
     if (j.nbeta % R != 0) continue;
     const int G = j.nbeta / R;
@@ -123,7 +132,7 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         q.phasor = ph;
         const size_t smem = plan_bytes<Model>(j, q, R, T, 1);
         if ((long long)smem > lim) continue;
-        const int n = dispatch_R(R, [&](auto rc) {
+        const int n = dispatch_R<Model>(R, [&](auto rc) {
           return sweep_capacity<Model, decltype(rc)::value>(G, T, smem, j.nseq);
         });
         if (n <= 0) continue;
@@ -199,7 +208,7 @@ int run_sweep(const cmc_job &j, cudaStream_t s, LaunchCfg *used = nullptr)
   if (rc) return rc;
   rc = Model::host_pack(j, pk, j.work, s);
   if (rc) return fail(rc, "packing the model data failed");
-  rc = dispatch_R(c.R, [&](auto rcnst) {
+  rc = dispatch_R<Model>(c.R, [&](auto rcnst) {
     return launch_sweep<Model, decltype(rcnst)::value>(j, pk, c, s);
   });
   if (used) *used = c;
@@ -224,13 +233,14 @@ int run_eval(const cmc_job &j, int mode, cudaStream_t s)
   size_t smem = 0;
   const int Rs[] = {4, 2, 1};
   for (int r : Rs) {
+    if (r > Model::kMaxR) continue;
     smem = plan_bytes<Model>(j, pk, r, T, 0);
     if ((long long)smem <= lim) { R = r; break; }
   }
   if (!R) return fail(CMC_ERR_UNSUPPORTED, "one replica's model rows do not fit in shared memory");
   rc = Model::host_pack(j, pk, j.work, s);
   if (rc) return fail(rc, "packing the model data failed");
-  return dispatch_R(R, [&](auto rcnst) {
+  return dispatch_R<Model>(R, [&](auto rcnst) {
     return launch_eval<Model, decltype(rcnst)::value>(j, pk, mode == 2 ? 1 : 0, T, smem, s);
   });
 }
@@ -242,6 +252,197 @@ size_t work_bytes(const cmc_job &j, int mode)
   const char *err = nullptr;
   if (Model::host_dims(j, mode, pk, &err)) return 0;
   return Model::host_work_bytes(pk);
+}
+
+// ---- batches of independent jobs (fits) ------------------------------------
+
+// One size class of a batch: one persistent batch-kernel launch whose work
+// list holds the (job, sequence) items of the class's jobs.
+struct BatchClass {
+  int R = 0, G = 0, T = 0, phasor = 0, item0 = 0, nitems = 0, nclusters = 0;
+  size_t smem = 0;
+};
+
+struct BatchPlan {
+  int njobs = 0, min_niter_total = 0;
+  std::vector<BatchClass> classes;
+  cmc_job *jobs_dev = nullptr;
+  void *pks_dev = nullptr;
+  int2 *items_dev = nullptr;
+  int *counters_dev = nullptr;
+  std::vector<cmc_job> jobs;        // host copies (kept for the uploads)
+  std::vector<unsigned char> pks;   // host copies of the packed descriptors
+  std::vector<int2> items;
+};
+
+constexpr int kBatchMaxClasses = 4;
+constexpr int kBatchClassLimit[kBatchMaxClasses] = {2048, 8192, 32768, 1 << 30};
+
+template <class Model>
+size_t batch_work_bytes(const cmc_job *jobs, int n)
+{
+  size_t items = 0;
+  for (int i = 0; i < n; ++i) items += (size_t)std::max(jobs[i].nseq, 0);
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  return al(sizeof(cmc_job) * n) + al(sizeof(typename Model::Packed) * n) + al(8 * items) +
+         al(4 * kBatchMaxClasses);
+}
+
+template <class Model>
+int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStream_t s,
+                  BatchPlan **out)
+{
+  using Packed = typename Model::Packed;
+  *out = nullptr;
+  if (!jobs || n < 1) return fail(CMC_ERR_ARG, "batch: need at least one job");
+  if (!work || bytes < batch_work_bytes<Model>(jobs, n))
+    return fail(CMC_ERR_ARG, "batch: work is smaller than cmc_batch_work_bytes()");
+  BatchPlan *P = new BatchPlan();
+  P->njobs = n;
+  P->jobs.assign(jobs, jobs + n);
+  P->pks.resize(sizeof(Packed) * n);
+  Packed *pk = reinterpret_cast<Packed *>(P->pks.data());
+  std::vector<int> npts(n);
+  P->min_niter_total = 1 << 30;
+  int rc = CMC_OK;
+  for (int i = 0; i < n; ++i) {
+    cmc_job v = jobs[i];
+    v.nburn = 0;
+    v.itr0 = 0;
+    v.niter = std::min(1, v.niter_total);
+    if ((rc = validate_common(v, 0)) != CMC_OK) break;
+    if (v.nbeta != jobs[0].nbeta) {
+      rc = fail(CMC_ERR_ARG, "batch: every job must have the same nbeta");
+      break;
+    }
+    const char *err = nullptr;
+    if ((rc = Model::host_dims(v, 0, pk[i], &err)) != CMC_OK) {
+      fail(rc, err);
+      break;
+    }
+    const size_t wb = Model::host_work_bytes(pk[i]);
+    if (wb > 0 && (v.work == nullptr || v.work_bytes < wb)) {
+      rc = fail(CMC_ERR_ARG, "batch: a job's work is smaller than cmc_work_bytes()");
+      break;
+    }
+    if ((rc = Model::host_pack(v, pk[i], v.work, s)) != CMC_OK) {
+      fail(rc, "batch: packing a job's data failed");
+      break;
+    }
+    npts[i] = Model::scratch_bytes(pk[i], 1);   // per-replica scratch: the size key
+    P->min_niter_total = std::min(P->min_niter_total, v.niter_total);
+  }
+  if (rc != CMC_OK) {
+    delete P;
+    return rc;
+  }
+  // size classes, each a work list sorted by decreasing cost (LPT)
+  const int lim = smem_optin();
+  const int nbeta = jobs[0].nbeta;
+  for (int c = 0; c < kBatchMaxClasses; ++c) {
+    const int lo = c ? kBatchClassLimit[c - 1] : -1, hi = kBatchClassLimit[c];
+    std::vector<int> mem;
+    for (int i = 0; i < n; ++i) {
+      const int key = (int)(npts[i] / 4);
+      if (key > lo && key <= hi) mem.push_back(i);
+    }
+    if (mem.empty()) continue;
+    std::stable_sort(mem.begin(), mem.end(), [&](int a, int b) {
+      return (double)npts[a] * (double)jobs[a].nseq > (double)npts[b] * (double)jobs[b].nseq;
+    });
+    int big = mem[0];
+    for (int i : mem)
+      if (npts[i] > npts[big]) big = i;
+    BatchClass bc;
+    double best = -1.0;
+    long long reps = 0;
+    for (int i : mem) reps += (long long)jobs[i].nseq * nbeta;
+    const int Rs[] = {1, 2, 4, 8, 16, 32};
+    for (int R : Rs) {
+      if (R > Model::kMaxR || nbeta % R || nbeta / R > 16) continue;
+      const int G = nbeta / R;
+      const int T = std::min(256, std::max(64, 32 * R));
+      for (int ph = 1; ph >= 0; --ph) {
+        Packed q = pk[big];
+        q.phasor = ph;
+        const size_t smem = plan_bytes<Model>(jobs[big], q, R, T, 1);
+        if ((long long)smem > lim) continue;
+        const int cap = dispatch_R<Model>(R, [&](auto rcn) {
+          return batch_capacity<Model, decltype(rcn)::value>(G, T, smem);
+        });
+        if (cap <= 0) continue;
+        const double resident = std::min((double)cap * nbeta, (double)reps);
+        const double score = resident * (ph ? 1.05 : 1.0);
+        if (score > best + 1e-9) {
+          best = score;
+          bc.R = R; bc.G = G; bc.T = T; bc.phasor = ph; bc.smem = smem; bc.nclusters = cap;
+        }
+      }
+    }
+    if (best < 0) {
+      delete P;
+      return fail(CMC_ERR_UNSUPPORTED, "batch: a job's data does not fit any launch shape "
+                                       "(too many points for shared memory)");
+    }
+    for (int i : mem) pk[i].phasor = bc.phasor;
+    bc.item0 = (int)P->items.size();
+    for (int i : mem)
+      for (int q = 0; q < jobs[i].nseq; ++q) P->items.push_back(make_int2(i, q));
+    bc.nitems = (int)P->items.size() - bc.item0;
+    bc.nclusters = std::min(bc.nclusters, bc.nitems);
+    // the descriptors' per-job smem must fit the class's launch
+    for (int i : mem) {
+      if (plan_bytes<Model>(jobs[i], pk[i], bc.R, bc.T, 1) > bc.smem) {
+        delete P;
+        return fail(CMC_ERR_UNSUPPORTED, "batch: inconsistent class shared-memory plan");
+      }
+    }
+    P->classes.push_back(bc);
+  }
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  unsigned char *w = (unsigned char *)work;
+  size_t o = 0;
+  P->jobs_dev = (cmc_job *)(w + o);   o += al(sizeof(cmc_job) * n);
+  P->pks_dev = (void *)(w + o);       o += al(sizeof(Packed) * n);
+  P->items_dev = (int2 *)(w + o);     o += al(8 * P->items.size());
+  P->counters_dev = (int *)(w + o);
+  cudaError_t e = cudaMemcpyAsync(P->jobs_dev, P->jobs.data(), sizeof(cmc_job) * n,
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->pks_dev, P->pks.data(), sizeof(Packed) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->items_dev, P->items.data(), 8 * P->items.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    delete P;
+    return cuda_fail(e, "batch: uploading the work lists");
+  }
+  *out = P;
+  return CMC_OK;
+}
+
+// Launches only (device-side state and work lists are ready): one memset and
+// one persistent kernel per size class, all on `s`.
+template <class Model>
+int batch_run(BatchPlan *P, int do_init, int nburn, int niter, int itr0, cudaStream_t s)
+{
+  using Packed = typename Model::Packed;
+  if (!P) return fail(CMC_ERR_ARG, "batch: plan is NULL");
+  if (nburn < 0 || niter < 0 || itr0 < 0 || itr0 + niter > P->min_niter_total)
+    return fail(CMC_ERR_ARG, "batch: need nburn, niter >= 0 and itr0 + niter <= niter_total");
+  for (size_t c = 0; c < P->classes.size(); ++c) {
+    const BatchClass &bc = P->classes[c];
+    CMC_CUDA(cudaMemsetAsync(P->counters_dev + c, 0, sizeof(int), s));
+    const int rc = dispatch_R<Model>(bc.R, [&](auto rcn) {
+      return launch_batch<Model, decltype(rcn)::value>(
+          P->jobs_dev, reinterpret_cast<const Packed *>(P->pks_dev), P->items_dev + bc.item0,
+          bc.nitems, P->counters_dev + c, bc.G, bc.T, bc.smem, bc.nclusters, do_init, nburn,
+          niter, itr0, s);
+    });
+    if (rc) return rc;
+  }
+  return CMC_OK;
 }
 
 // ---- the reference's host-pointer entry points ------------------------------

@@ -26,6 +26,15 @@ template <class Model, int R>
 int launch_sweep(const cmc_job &j, const typename Model::Packed &pk, const LaunchCfg &c,
                  cudaStream_t s);
 
+// Resident clusters of the batch kernel at this shape (0: does not fit).
+template <class Model, int R>
+int batch_capacity(int G, int T, size_t smem);
+
+template <class Model, int R>
+int launch_batch(const cmc_job *jobs, const typename Model::Packed *pks, const int2 *items,
+                 int nitems, int *counter, int G, int T, size_t smem, int nclusters, int do_init,
+                 int nburn, int niter, int itr0, cudaStream_t s);
+
 template <class Model, int R>
 int launch_eval(const cmc_job &j, const typename Model::Packed &pk, int model_only, int T,
                 size_t smem, cudaStream_t s);

@@ -74,6 +74,69 @@ int launch_sweep(const cmc_job &j, const typename Model::Packed &pk, const Launc
 }
 
 template <class Model, int R>
+int batch_capacity(int G, int T, size_t smem)
+{
+  auto kern = batch_kernel<Model, R>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (G > 8 &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(G);
+  cfg.blockDim = dim3(T);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, (void *)kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+template <class Model, int R>
+int launch_batch(const cmc_job *jobs, const typename Model::Packed *pks, const int2 *items,
+                 int nitems, int *counter, int G, int T, size_t smem, int nclusters, int do_init,
+                 int nburn, int niter, int itr0, cudaStream_t s)
+{
+  auto kern = batch_kernel<Model, R>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && G > 8)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("batch kernel attributes: ") + cudaGetErrorString(e));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(G * nclusters);
+  cfg.blockDim = dim3(T);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, jobs, pks, items, nitems, counter, do_init, nburn, niter,
+                         itr0);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("batch kernel launch: ") + cudaGetErrorString(e));
+  return CMC_OK;
+}
+
+template <class Model, int R>
 int launch_eval(const cmc_job &j, const typename Model::Packed &pk, int model_only, int T,
                 size_t smem, cudaStream_t s)
 {
@@ -94,6 +157,10 @@ int launch_eval(const cmc_job &j, const typename Model::Packed &pk, int model_on
   template int launch_sweep<MODEL, RV>(const cmc_job &, const MODEL::Packed &,           \
                                        const LaunchCfg &, cudaStream_t);                  \
   template int launch_eval<MODEL, RV>(const cmc_job &, const MODEL::Packed &, int, int,  \
-                                      size_t, cudaStream_t);
+                                      size_t, cudaStream_t);                              \
+  template int batch_capacity<MODEL, RV>(int, int, size_t);                               \
+  template int launch_batch<MODEL, RV>(const cmc_job *, const MODEL::Packed *, const int2 *, \
+                                       int, int *, int, int, size_t, int, int, int, int, int, \
+                                       cudaStream_t);
 
 }  // namespace cmc

@@ -12,15 +12,14 @@ namespace cmc {
 #define CMC_MIN_BLOCKS 2
 #endif
 
+// One sequence iseq of `job` on the calling cluster (all its CTAs call this
+// with the same arguments).  `smem` is the CTA's dynamic shared memory, at
+// least make_plan(...).total bytes for this job.
 template <class Model, int R>
-__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
-sweep_kernel(const cmc_job job, const typename Model::Packed pk)
+__device__ void run_sequence(const cmc_job &job, const typename Model::Packed &pk, int iseq,
+                             cg::cluster_group &cluster, unsigned char *smem)
 {
-  extern __shared__ __align__(16) unsigned char smem[];
-  cg::cluster_group cluster = cg::this_cluster();
-  const int G = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
-  const int iseq = blockIdx.x / G;
   const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
   const int nbeta = job.nbeta, nseq = job.nseq, nptot = job.nptot, nprm = job.nprm;
   const int nadj = job.nadj;
@@ -369,8 +368,62 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
   }
   // Model rows of each replica's last evaluation (datm / chi2m outputs).
   Model::template final_rows<R>(cta, plast, s_evald);
-  // No CTA may leave while another can still read its shared memory.
+  // No CTA may leave (or start its next sequence) while another can still
+  // read its shared memory.
   cluster.sync();
+}
+
+// One launch for one job: cluster c runs sequence c.
+template <class Model, int R>
+__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
+sweep_kernel(const cmc_job job, const typename Model::Packed pk)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  cg::cluster_group cluster = cg::this_cluster();
+  run_sequence<Model, R>(job, pk, blockIdx.x / (int)cluster.num_blocks(), cluster, smem);
+}
+
+// Persistent launch over a work list of (job, sequence) items of many
+// independent jobs (fits): each cluster takes the next item from an atomic
+// counter (the list is sorted by decreasing cost, so the tail is short),
+// copies that job's descriptor into shared memory, applies this launch's
+// iteration window (do_init, nburn, niter, itr0) and runs the sequence.
+template <class Model, int R>
+__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
+batch_kernel(const cmc_job *jobs, const typename Model::Packed *pks, const int2 *items,
+             int nitems, int *counter, int do_init, int nburn, int niter, int itr0)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ cmc_job s_job;
+  __shared__ typename Model::Packed s_pk;
+  __shared__ int s_item;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  for (;;) {
+    if (rank == 0 && threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    cluster.sync();
+    const int it = *cluster.map_shared_rank(&s_item, 0);
+    cluster.sync();
+    if (it >= nitems) break;
+    const int2 w = items[it];
+    {
+      const int *src = reinterpret_cast<const int *>(&jobs[w.x]);
+      int *dst = reinterpret_cast<int *>(&s_job);
+      for (int i = threadIdx.x; i < (int)(sizeof(cmc_job) / 4); i += blockDim.x) dst[i] = src[i];
+      const int *psrc = reinterpret_cast<const int *>(&pks[w.x]);
+      int *pdst = reinterpret_cast<int *>(&s_pk);
+      for (int i = threadIdx.x; i < (int)(sizeof(s_pk) / 4); i += blockDim.x) pdst[i] = psrc[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_job.do_init = do_init;
+      s_job.nburn = nburn;
+      s_job.niter = niter;
+      s_job.itr0 = itr0;
+    }
+    __syncthreads();
+    run_sequence<Model, R>(s_job, s_pk, w.y, cluster, smem);
+  }
 }
 
 }  // namespace cmc

@@ -24,6 +24,7 @@ struct PluginModel {
   struct Packed { int ndat, npass, phasor; };
 
   static constexpr bool kRowsInEval = true;
+  static constexpr int kMaxR = 32;  // instantiated replicas-per-CTA counts: 1 .. 32
 
   __host__ __device__ static unsigned scratch_bytes(const Packed &, int)
   {

@@ -109,6 +109,7 @@ struct SgraModel {
   };
 
   static constexpr bool kRowsInEval = false;
+  static constexpr int kMaxR = 8;   // instantiated replicas-per-CTA counts: 1, 2, 4, 8
   static constexpr unsigned kTabBytes =
       (unsigned)sizeof(float4) * kBesselIntervals * ((kBesselDeg + 1) / 2);
 

@@ -155,6 +155,7 @@ class DeviceJob:
         j.work, j.work_bytes = _ptr(t["work"]), wb
         self.job = j
         self.itr_done = 0
+        self.shape = None          # forced launch shape {R, T, phasor} (see autotune.py)
 
     @classmethod
     def from_workload(cls, w, niter_total=None, seed=1234, rng="curand", streams=None,
@@ -175,8 +176,19 @@ class DeviceJob:
         j.nburn, j.niter = int(nburn), int(niter)
         j.itr0 = self.itr_done if itr0 is None else int(itr0)
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
-        _lib.check(self.L, self.L.cmc_run(C.byref(j), C.c_void_p(s.cuda_stream)))
+        if self.shape:
+            self.L.cmc_set_config(self.shape["R"], self.shape["T"], self.shape["phasor"])
+        try:
+            _lib.check(self.L, self.L.cmc_run(C.byref(j), C.c_void_p(s.cuda_stream)))
+        finally:
+            if self.shape:
+                self.L.cmc_set_config(0, 0, -1)
         self.itr_done = j.itr0 + j.niter
+
+    def autotune(self, **kw):
+        """Time every feasible launch shape on this job and keep the fastest."""
+        from . import autotune
+        return autotune.tune(self, **kw)
 
     def eval(self, mode=_lib.MODE_MODCHI2, stream=None):
         """calc_modchi2 (mode 1) / calc_model (mode 2) on the current pcur."""
@@ -191,12 +203,18 @@ class DeviceJob:
             raise _lib.McmcError(st, "device status %d (see cmc_status in cmc_job.h)" % st)
 
     def config(self):
-        """Launch shape the library picks for this job: (R, G, T, phasor, smem, clusters/wave)."""
+        """Launch shape used for this job: (R, G, T, phasor, smem, clusters/wave)."""
         R, G, T, P, W = (C.c_int() for _ in range(5))
         sm = C.c_size_t()
-        _lib.check(self.L, self.L.cmc_query_config(C.byref(self.job), C.byref(R), C.byref(G),
-                                                   C.byref(T), C.byref(P), C.byref(sm),
-                                                   C.byref(W)))
+        if self.shape:
+            self.L.cmc_set_config(self.shape["R"], self.shape["T"], self.shape["phasor"])
+        try:
+            _lib.check(self.L, self.L.cmc_query_config(C.byref(self.job), C.byref(R), C.byref(G),
+                                                       C.byref(T), C.byref(P), C.byref(sm),
+                                                       C.byref(W)))
+        finally:
+            if self.shape:
+                self.L.cmc_set_config(0, 0, -1)
         return dict(R=R.value, G=G.value, T=T.value, phasor=P.value, smem=sm.value,
                     clusters_per_wave=W.value)
 
@@ -214,3 +232,71 @@ class DeviceJob:
             dst = self.t[k]
             src = torch.as_tensor(np.ascontiguousarray(v)).to(dtype=dst.dtype).reshape(dst.shape)
             dst.copy_(src.to(self.device))
+
+
+class BatchJob:
+    """Many independent fits of one model (DeviceJobs with the same nbeta) run
+    by persistent work-list launches: the (fit, sequence) items are split into
+    size classes, each class one launch whose clusters take items from an
+    atomic counter, largest first.  ``run()`` only launches (the descriptors
+    and work lists are built once here), so a chunk loop can be captured in a
+    CUDA graph."""
+
+    def __init__(self, jobs, stream=None):
+        if not jobs:
+            raise ValueError("BatchJob needs at least one DeviceJob")
+        self.jobs = list(jobs)
+        self.L = self.jobs[0].L
+        self.device = self.jobs[0].device
+        if any(j.L is not self.L for j in self.jobs):
+            raise ValueError("all jobs of a batch must use the same model library")
+        n = len(self.jobs)
+        arr = (_lib.CmcJob * n)(*[j.job for j in self.jobs])
+        wb = int(self.L.cmc_batch_work_bytes(arr, n))
+        self.work = torch.zeros(max(wb, 16), dtype=_U8, device=self.device)
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        plan = self.L.cmc_batch_prepare(arr, n, C.c_void_p(self.work.data_ptr()), wb,
+                                        C.c_void_p(s.cuda_stream))
+        if not plan:
+            raise _lib.McmcError(_lib.CMC_ERR_ARG, self.L.cmc_last_error().decode())
+        self.plan = C.c_void_p(plan)
+        self.itr_done = 0
+
+    def run(self, nburn=0, niter=0, do_init=False, itr0=None, stream=None):
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        i0 = self.itr_done if itr0 is None else int(itr0)
+        _lib.check(self.L, self.L.cmc_batch_run(self.plan, 1 if do_init else 0, int(nburn),
+                                                int(niter), i0, C.c_void_p(s.cuda_stream)))
+        self.itr_done = i0 + int(niter)
+
+    def graph(self, nburn=0, niter=0, itr0=0):
+        """Capture one chunk (memsets + one persistent launch per size class)
+        as a CUDA graph; replaying it runs the chunk again (recording main
+        iterations at column itr0 each time)."""
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.graph(g, stream=side):
+            self.run(nburn, niter, itr0=itr0, stream=side)
+        return g
+
+    def classes(self):
+        out = []
+        n = self.L.cmc_batch_info(self.plan, -1, None, None, None, None, None, None, None)
+        for c in range(n):
+            v = [C.c_int() for _ in range(6)]
+            sm = C.c_size_t()
+            self.L.cmc_batch_info(self.plan, c, *[C.byref(x) for x in v], C.byref(sm))
+            out.append(dict(R=v[0].value, G=v[1].value, T=v[2].value, phasor=v[3].value,
+                            items=v[4].value, clusters=v[5].value, smem=sm.value))
+        return out
+
+    def check(self):
+        for j in self.jobs:
+            j.check()
+
+    def __del__(self):
+        plan = getattr(self, "plan", None)
+        if plan is not None and plan.value:
+            self.L.cmc_batch_free(plan)
+            self.plan = None

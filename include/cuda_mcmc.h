@@ -113,6 +113,27 @@ int cmc_run_noalloc(const cmc_job *job, void *stream);
  * mode 2 = calc_model.  Asynchronous on `stream`. */
 int cmc_eval(const cmc_job *job, int mode, void *stream);
 
+/* ---- batches of independent jobs (fits) ------------------------------------
+ * No counterpart in the reference (it runs one fit per mcmc_cuda call).
+ * Every job is a complete cmc_job (device arrays, own sizes; all with the same
+ * nbeta).  cmc_batch_prepare validates the jobs, packs their data (each job's
+ * own job->work), splits the (job, sequence) items into size classes and
+ * uploads the descriptors and work lists into `work` (cmc_batch_work_bytes
+ * bytes, caller-owned device memory); it returns an opaque plan (NULL on
+ * error, see cmc_last_error).  cmc_batch_run then only launches: one
+ * persistent kernel per size class whose clusters take items, largest first,
+ * from an atomic counter, with this launch's iteration window (do_init, nburn,
+ * niter, itr0) applied to every job; it can be captured in a CUDA graph.
+ * cmc_batch_info reports class `cls`'s launch shape (returns the number of
+ * classes); cmc_batch_free releases the host-side plan. */
+size_t cmc_batch_work_bytes(const cmc_job *jobs, int njobs);
+void *cmc_batch_prepare(const cmc_job *jobs, int njobs, void *work, size_t work_bytes,
+                        void *stream);
+int cmc_batch_run(void *plan, int do_init, int nburn, int niter, int itr0, void *stream);
+int cmc_batch_info(void *plan, int cls, int *R, int *G, int *T, int *phasor, int *nitems,
+                   int *nclusters, size_t *smem);
+void cmc_batch_free(void *plan);
+
 /* Bytes of library scratch (packed data of the built-in fast models) that
  * job->work must provide for cmc_run (mode 0) or cmc_eval (mode 1, 2).  The
  * reference allocates its device buffers itself (src/mcmcjob.cu:689-718). */

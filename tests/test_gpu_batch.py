@@ -1,0 +1,71 @@
+"""The batched persistent path (many independent fits in work-list launches).
+
+Each fit of a batch must walk exactly the chain it walks alone: with the same
+seed and the same launch shape (the shape of its size class), the batch and a
+single-job run of that fit give bit-identical outputs.  The chi^2 traces are
+also checked against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cuda_mcmc_gb300 import _lib, synth
+from cuda_mcmc_gb300.device import BatchJob, DeviceJob
+
+pytestmark = pytest.mark.gpu
+
+CHI2_RTOL = 1e-5
+
+
+def _fits():
+    # sizes spread over the batch size classes
+    sizes = [(120, 36), (700, 210), (2500, 750), (5200, 1560)]
+    return [synth.sgra(nvis=nv, ncph=nc, seed=50 + i, nseq=3, nbeta=16)
+            for i, (nv, nc) in enumerate(sizes)]
+
+
+def test_batch_equals_individual_runs_with_the_class_shape():
+    fits = _fits()
+    nburn, niter = 6, 8
+    jobs = [DeviceJob.from_workload(w, niter_total=niter, seed=100 + i) for i, w in enumerate(fits)]
+    batch = BatchJob(jobs)
+    classes = batch.classes()
+    assert sum(c["items"] for c in classes) == sum(w.nseq for w in fits)
+    batch.run(nburn, 0, do_init=True)
+    batch.run(0, niter)
+    batch.check()
+    # which class (shape) each fit landed in: classes are filled in size order
+    for i, w in enumerate(fits):
+        got = jobs[i].to_numpy()
+        ref = DeviceJob.from_workload(w, niter_total=niter, seed=100 + i)
+        matched = False
+        for c in classes:
+            ref2 = DeviceJob.from_workload(w, niter_total=niter, seed=100 + i)
+            ref2.shape = {"R": c["R"], "T": c["T"], "phasor": c["phasor"]}
+            try:
+                ref2.run(nburn, 0, do_init=True)
+                ref2.run(0, niter)
+                ref2.check()
+            except _lib.McmcError:
+                continue
+            r = ref2.to_numpy()
+            if np.array_equal(r["pout"], got["pout"]) and np.array_equal(r["rndst"], got["rndst"]):
+                for f in ("chi2", "tout", "pcur", "chi2c", "n_acpt", "n_exch", "n_hist", "pstp"):
+                    assert np.array_equal(r[f], got[f]), f
+                matched = True
+                break
+        assert matched, "fit %d: the batch result matches no single-job run" % i
+        # chi^2 trace vs FP64 oracle
+        pb = oracle.Problem(w.model, w.coor, w.dat, w.std2r, w.icoor, w.idat, w.nptot,
+                            w.imodel, w.npass)
+        P = np.stack([got["pout"][:, 0, q, it] for q in range(w.nseq) for it in (0, niter - 1)])
+        _, _, _, c2 = oracle.calc_modchi2(pb, P.astype(np.float32))
+        c2g = np.array([got["chi2"][q, it] for q in range(w.nseq) for it in (0, niter - 1)])
+        assert np.max(np.abs(c2g - c2) / c2) < CHI2_RTOL
+
+
+def test_batch_rejects_mixed_nbeta():
+    a = DeviceJob.from_workload(synth.sgra(nvis=100, ncph=30, nseq=2, nbeta=8), niter_total=1)
+    b = DeviceJob.from_workload(synth.sgra(nvis=100, ncph=30, nseq=2, nbeta=16), niter_total=1)
+    with pytest.raises(_lib.McmcError, match="nbeta"):
+        BatchJob([a, b])
