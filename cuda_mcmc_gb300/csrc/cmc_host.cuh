@@ -361,7 +361,10 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
     for (int R : Rs) {
       if (R > Model::kMaxR || nbeta % R || nbeta / R > 16) continue;
       const int G = nbeta / R;
-      const int T = std::min(256, std::max(64, 32 * R));
+      // ~32 threads per replica, and never fewer than one thread per 16
+      // points of the class's largest job
+      const int want = std::max(32 * R, (int)std::min<long long>(256, Model::points(pk[big]) / 16));
+      const int T = want <= 64 ? 64 : want <= 128 ? 128 : 256;
       for (int ph = 1; ph >= 0; --ph) {
         Packed q = pk[big];
         q.phasor = ph;

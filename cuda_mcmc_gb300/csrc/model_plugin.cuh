@@ -26,6 +26,9 @@ struct PluginModel {
   static constexpr bool kRowsInEval = true;
   static constexpr int kMaxR = 32;  // instantiated replicas-per-CTA counts: 1 .. 32
 
+  // data points one replica's evaluation runs over
+  __host__ __device__ static int points(const Packed &pk) { return pk.ndat * pk.npass; }
+
   __host__ __device__ static unsigned scratch_bytes(const Packed &, int)
   {
     return (unsigned)sizeof(CCalcModel);

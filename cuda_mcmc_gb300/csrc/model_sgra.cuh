@@ -113,6 +113,9 @@ struct SgraModel {
   static constexpr unsigned kTabBytes =
       (unsigned)sizeof(float4) * kBesselIntervals * ((kBesselDeg + 1) / 2);
 
+  // data points one replica's evaluation runs over
+  __host__ __device__ static int points(const Packed &pk) { return pk.npts + pk.ncph; }
+
   // shared scratch: Bessel table, then phasors [R][npts] (float2) or phases (float)
   __host__ __device__ static unsigned scratch_bytes(const Packed &pk, int R)
   {

@@ -246,3 +246,44 @@ def config(i: int) -> Workload:
     if i == 4:
         return sgra(nvis=20000, ncph=6000, seed=4)
     raise ValueError("config must be 1-4 (5 is sgra_batch())")
+
+
+def write_uvdata(path, nant=5, ntimes=40, t0="2009:095:02:20:00", dt_s=1200, seed=9,
+                 truth=None, snr_amp=0.03, imodel=1):
+    """Write a synthetic observation in the uv text format read by
+    imgpu.read_uvdata (one row per baseline and time: time, u v w in
+    kilolambda, baseline aa-bb, channel, (amplitude, phase in degrees),
+    weight, sigma).  All baselines of nant stations are present at every time,
+    so every antenna triangle gives a closure phase.  Returns the true
+    parameters and the (u, v) points in gigalambda."""
+    import calendar
+    import time as _time
+    rng = np.random.default_rng(seed)
+    if truth is None:
+        truth = sgra_truth(rng)
+    truth = np.asarray(truth, np.float32)
+    # station positions on a ~8 Glambda disk; baselines rotate with time
+    pos = rng.uniform(-4.0, 4.0, (nant, 2))
+    base = calendar.timegm(_time.strptime(t0, "%Y:%j:%H:%M:%S"))
+    rows, uvs = [], []
+    for it in range(ntimes):
+        ang = 2 * np.pi * it / (4 * ntimes)
+        rot = np.array([[np.cos(ang), -np.sin(ang)], [np.sin(ang), np.cos(ang)]])
+        p = pos @ rot.T
+        ts = _time.strftime("%Y:%j:%H:%M:%S", _time.gmtime(base + it * dt_s))
+        for a in range(nant):
+            for b in range(a + 1, nant):
+                u, v = p[a] - p[b]
+                uvs.append((u, v))
+                rows.append((ts, u, v, a + 1, b + 1))
+    uv = np.array(uvs)
+    amp, pha = _sgra9_vis_np(truth, uv[:, 0], uv[:, 1])
+    sig = snr_amp * amp + 0.002
+    amp_obs = amp * (1 + snr_amp * rng.standard_normal(amp.size))
+    with open(path, "w") as f:
+        f.write("Scan Start (UT)  U(klam)  V(klam)  W(klam)  Baseline  Channel  "
+                "Visibility (amp, phase)  Weight  Sigma\n")
+        for (ts, u, v, a, b), am, ph, sg in zip(rows, amp_obs, pha, sig):
+            f.write("%s.00 %13.2f %13.2f %13.2f %02d-%02d    00    ( %12.6f, %15.6f) %9.2f %.5f\n"
+                    % (ts, u * 1e6, v * 1e6, 0.0, a, b, am, np.degrees(ph), 1000.0, sg))
+    return truth, uv

@@ -1,0 +1,121 @@
+"""The high-level Python API (imgpu) and its data helpers.
+
+CPU: uv-file parsing, closure building, the reference's defaults in the
+Mcgpu state.  GPU: the examples' compute sections through Mcgpu /
+Mcgpu_Sgra, checked against the FP64 oracle.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from cuda_mcmc_gb300 import imgpu, synth
+
+REF_UV = sorted(glob.glob("/root/reference/examples/sgra_model_fit/*_uvdata.txt"))
+
+
+def _wrap(x):
+    return np.angle(np.exp(1j * x))
+
+
+def test_read_uvdata_roundtrip(tmp_path):
+    f = str(tmp_path / "obs_uvdata.txt")
+    truth, uv = synth.write_uvdata(f, nant=5, ntimes=6)
+    ulam, vlam, wlam, amp, phase, blin, tsec, sig, chan, wei = imgpu.read_uvdata(f)
+    assert ulam.size == uv.shape[0] == 6 * 10
+    # file in kilolambda -> megalambda here; the Sgr A* class scales to Glambda
+    assert np.allclose(1e-3 * ulam, uv[:, 0], atol=1e-5)
+    assert np.allclose(1e-3 * vlam, uv[:, 1], atol=1e-5)
+    assert np.all(np.abs(phase) <= np.pi + 1e-6)
+    assert blin.shape == (60, 2) and blin.min() == 1 and blin.max() == 5
+    assert len(set(tsec.tolist())) == 6
+    assert np.all(sig > 0)
+
+
+def test_calc_closures_triangles(tmp_path):
+    f = str(tmp_path / "obs_uvdata.txt")
+    synth.write_uvdata(f, nant=5, ntimes=4)
+    _, _, _, amp, phase, blin, tsec, _, _, _ = imgpu.read_uvdata(f)
+    cphs, cpix, trid, tcp = imgpu.calc_closures(phase, tsec, blin)
+    assert cphs.size == 4 * imgpu.cbinom(5, 3)
+    ref = phase[cpix[:, 0]] + phase[cpix[:, 1]] - phase[cpix[:, 2]]
+    assert np.allclose(_wrap(cphs - ref), 0, atol=1e-6)
+    # triangle (a1, a2, a3): rows are baselines a1-a2, a1-a3, a2-a3
+    assert np.all(blin[cpix[:, 0], 0] == blin[cpix[:, 1], 0])
+    assert np.all(blin[cpix[:, 0], 1] == blin[cpix[:, 2], 0])
+    assert np.all(blin[cpix[:, 1], 1] == blin[cpix[:, 2], 1])
+
+
+def test_helpers():
+    assert imgpu.cbinom(6, 3) == 20 and imgpu.cbinom(2, 3) == -1
+    c = imgpu.combgen(6, 3)
+    assert c.shape == (20, 3) and c[5].tolist() == [0, 2, 4]
+    ib, ie = imgpu.get_time_indices(np.array([0, 0, 0, 1, 1, 2, 2, 2, 2], float))
+    assert ib == [0, 5] and ie == [3, 9]
+
+
+@pytest.mark.skipif(not REF_UV, reason="reference uv files not present")
+def test_read_reference_uv_files():
+    for f in REF_UV:
+        ulam, vlam, wlam, amp, phase, blin, tsec, sig, chan, wei = imgpu.read_uvdata(f)
+        assert 200 < ulam.size < 400
+        base = 1e-3 * np.sqrt(ulam ** 2 + vlam ** 2)
+        assert base.max() < 12.0
+        cphs, cpix, trid, tcp = imgpu.calc_closures(phase, tsec, blin)
+        assert cphs.size > 0
+        ref = phase[cpix[:, 0]] + phase[cpix[:, 1]] - phase[cpix[:, 2]]
+        assert np.allclose(_wrap(cphs - ref), 0, atol=1e-5)
+
+
+def test_mcgpu_defaults_follow_the_reference():
+    m = imgpu.Mcgpu(coor=np.array([2, 2, 0.25, 0.5], np.float32), dat=np.array([1, 0.5]),
+                    pdescr=np.array([1, 1]), pmint=np.array([-5.0, -5.0]),
+                    pmaxt=np.array([5.0, 5.0]), nbeta=8, nseq=3, seed=1, model="solvsys")
+    assert m.pcur.shape == (8, 3, 2) and np.all(m.pcur == 0.0)
+    assert np.allclose(m.pstp, 0.2)
+    assert m.beta[0] == 1.0 and np.isclose(m.beta[-1], 1e-4, rtol=1e-5)
+    assert np.all(m.n_cnt == 1) and m.tcur[:, 1].tolist() == list(range(8))
+    assert m.ndatm == 8 * 3 * 2 and m.invar.tolist() == [0, 1]
+
+
+@pytest.mark.gpu
+def test_solvsys_example_replay():
+    """examples/solvsys/solvsys.py:38-62 through imgpu.Mcgpu."""
+    m = imgpu.Mcgpu(coor=np.array([2, 2, 0.25, 0.5], np.float32), dat=np.array([1, 0.5]),
+                    pdescr=np.array([1, 1]), pmint=np.array([-5.0, -5.0]),
+                    pmaxt=np.array([5.0, 5.0]), nbeta=32, nseq=14, nburn=400, niter=5000,
+                    seed=3, model="solvsys")
+    m.burnin_and_search()
+    assert m.pout.shape == (2, 14 * 5000) and m.chi2.shape == (14 * 5000,)
+    best = m.pout[:, m.chi2 < 0.0002]
+    rx = np.array([(-4.0 - np.sqrt(832.0)) / 34.0, (-4.0 + np.sqrt(832.0)) / 34.0])
+    assert best.shape[1] > 0
+    assert np.all(np.min(np.abs(best[0][:, None] - rx[None]), axis=1) < 0.05)
+    assert m.rate_acpt.shape == (32, 14)
+
+
+@pytest.mark.gpu
+def test_sgra_fit_from_uv_file(tmp_path):
+    f = str(tmp_path / "obs_uvdata.txt")
+    truth, uv = synth.write_uvdata(f, nant=6, ntimes=20, seed=4)
+    m = imgpu.Mcgpu_Sgra(f, imodel=1, nseq=4, nbeta=16, nburn=40, niter=60, seed=11,
+                         pdescr=synth.SGRA9_PDESCR, pmint=synth.SGRA9_PMIN,
+                         pmaxt=synth.SGRA9_PMAX, ecph=np.radians(5.0))
+    assert m.error == "" and m.cpExt == 0 and m.ncph == 20 * imgpu.cbinom(6, 3)
+    assert m.burnin_and_search() == 0
+    # the recorded chi^2 of a sample equals calcmodchi2 of it, and FP64
+    k = int(np.argmin(m.chi2))
+    p = m.pout[:, k].astype(np.float32)
+    chi2c, mvicp, mpha, chi2m, datm = m.calcmodchi2(p)
+    assert np.isclose(chi2c, m.chi2[k], rtol=1e-5)
+    pb = oracle.Problem("sgra", m.coor, m.dat, m.std2r, m.icoor, m.idat, 9, 1, 2)
+    _, _, _, c2 = oracle.calc_modchi2(pb, p[None])
+    assert np.isclose(chi2c, c2[0], rtol=1e-5)
+    # calcmodel on a grid, interleaved layout, against FP64
+    g = np.linspace(-6, 6, 9).astype(np.float32)
+    U, V = np.meshgrid(g, g)
+    mamp, mph = m.calcmodel(U, V, p, imodel=1, uv_layout="interleaved")
+    a, ph = oracle.sgra_vis(1, p, U.ravel(), V.ravel())
+    assert np.max(np.abs(mamp.ravel() - a) - 1e-5 * a) <= 1e-6 * p[0]
