@@ -113,6 +113,11 @@ def _declare(L):
     L.cmc_batch_info.restype = C.c_int
     L.cmc_batch_free.argtypes = [C.c_void_p]
     L.cmc_batch_free.restype = None
+    if hasattr(L, "cmc_grad"):          # Sgr A* library only
+        L.cmc_grad_work_bytes.argtypes = [C.POINTER(CmcJob)]
+        L.cmc_grad_work_bytes.restype = C.c_size_t
+        L.cmc_grad.argtypes = [C.POINTER(CmcJob), C.c_void_p, C.c_void_p]
+        L.cmc_grad.restype = C.c_int
     if L.cmc_sizeof_job() != C.sizeof(CmcJob):
         raise RuntimeError("cmc_job layout mismatch between %s and _lib.CmcJob" % L._name)
 

@@ -97,7 +97,7 @@ __device__ __forceinline__ void bessel_f12_tab(const float4 *tab, float x, float
     const float ix = 1.0f / x;
     const float j0 = j0f(x), j1 = j1f(x);
     f1 = j1 * ix;
-    f2 = (2.0f * f1 - j0) * ix * ix;
+    f2 = fmaf(2.0f, f1, -j0) * ix * ix;
   }
 }
 

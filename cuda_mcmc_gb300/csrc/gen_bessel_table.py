@@ -1,5 +1,6 @@
 """Generate bessel_table.cuh: piecewise polynomials for
     F1(x) = J1(x) / x      and      F2(x) = J2(x) / x^2
+(and, for derivatives, F3(x) = J3(x) / x^3: F1' = -x F2, F2' = -x F3)
 on x in [0, XMAX) in unit intervals [i, i+1), each a degree-DEG polynomial in
 d = x - (i + 0.5).  Both functions are entire and even, with F1(0) = 1/2 and
 F2(0) = 1/8.
@@ -43,6 +44,15 @@ def f2(x):
     return out
 
 
+def f3(x):
+    x = np.asarray(x, np.float64)
+    out = np.empty_like(x)
+    small = np.abs(x) < 1e-2
+    out[small] = 1.0 / 48 - x[small] ** 2 / 768
+    out[~small] = jv(3, x[~small]) / x[~small] ** 3
+    return out
+
+
 def fit(fun, i):
     c = i + 0.5
     # Chebyshev nodes on d in [-1/2, 1/2]
@@ -64,13 +74,14 @@ def horner32(coef, d):
 
 
 def main():
-    tab = np.zeros((XMAX, DEG + 1, 2), np.float32)
-    err = [0.0, 0.0]
+    tab = np.zeros((XMAX, DEG + 1, 3), np.float32)
+    err = [0.0, 0.0, 0.0]
     for i in range(XMAX):
         tab[i, :, 0] = fit(f1, i)
         tab[i, :, 1] = fit(f2, i)
+        tab[i, :, 2] = fit(f3, i)
         xs = np.linspace(i, i + 1, 401)[:-1]
-        for j, fun in enumerate((f1, f2)):
+        for j, fun in enumerate((f1, f2, f3)):
             ref = fun(xs)
             got = np.array([horner32(tab[i, :, j], np.float32(x) - np.float32(i + 0.5))
                             for x in xs], np.float64)
@@ -82,7 +93,7 @@ def main():
         "// coefficients a_k (k = 0..%d) of sum_k a_k d^k, d = x - (i + 0.5), stored as" % DEG,
         "// float4 (F1 a_2m, F2 a_2m, F1 a_2m+1, F2 a_2m+1), m = 0..%d.  Chebyshev" % ((DEG - 1) // 2),
         "// interpolants of float64 values, rounded",
-        "// to float32; max |error| with float32 Horner: F1 %.2e, F2 %.2e." % tuple(err),
+        "// to float32; max |error| with float32 Horner: F1 %.2e, F2 %.2e." % tuple(err[:2]),
         "#pragma once",
         "",
         "namespace cmc {",
@@ -95,10 +106,16 @@ def main():
                                                            tab[i, 2 * m + 1, 0], tab[i, 2 * m + 1, 1])
                         for m in range((DEG + 1) // 2))
         lines.append("    {%s}," % row)
+    lines += ["};", "",
+              "// F3(x) = J3(x)/x^3, same intervals, coefficients a_0..a_%d (max |error| %.2e)."
+              % (DEG, err[2]),
+              "static __device__ const float kBesselTab3[%d][%d] = {" % (XMAX, DEG + 1)]
+    for i in range(XMAX):
+        lines.append("    {%s}," % ", ".join("%.9ef" % tab[i, k, 2] for k in range(DEG + 1)))
     lines += ["};", "}  // namespace cmc", ""]
     with open(os.path.join(HERE, "bessel_table.cuh"), "w") as f:
         f.write("\n".join(lines))
-    print("max abs error: F1 %.3e  F2 %.3e" % tuple(err))
+    print("max abs error: F1 %.3e  F2 %.3e  F3 %.3e" % tuple(err))
 
 
 if __name__ == "__main__":

@@ -69,3 +69,69 @@ extern "C" int cmc_run_noalloc(const cmc_job *job, void *stream)
   j.work_bytes = kStaticWorkBytes;
   return cmc::run_sweep<cmc::SgraModel>(j, (cudaStream_t)stream);
 }
+
+// ---- chi^2 gradient (no counterpart in the reference) -----------------------
+//
+// cmc_grad: chi2c[ist] and dchi2/dp into grad[ist*nptot + k] at pcur for every
+// replica ist < nbeta*nseq (flag[ist] == 0 with flag non-NULL: zeros), with the
+// job's npass (npass < 2: amplitude terms only).  job->work holds the packed
+// data followed by the per-point phases and adjoints of every replica:
+// cmc_grad_work_bytes(job) bytes.
+#include "model_sgra_grad.cuh"
+
+namespace {
+size_t grad_extra_offset(const cmc::SgraModel::Packed &pk)
+{
+  return (cmc::SgraModel::host_work_bytes(pk) + 255) & ~(size_t)255;
+}
+
+int grad_dims(const cmc_job &j, cmc::SgraModel::Packed &pk)
+{
+  int rc = cmc::validate_common(j, 1);
+  if (rc) return rc;
+  const char *err = nullptr;
+  cmc_job k = j;
+  k.datm = nullptr;   // the gradient writes no model rows
+  rc = cmc::SgraModel::host_dims(k, 0, pk, &err);
+  if (rc) return cmc::fail(rc, err);
+  if (j.nptot > cmc::kMaxGradParams)
+    return cmc::fail(CMC_ERR_ARG, "cmc_grad: nptot must be <= 16");
+  return CMC_OK;
+}
+}  // namespace
+
+extern "C" size_t cmc_grad_work_bytes(const cmc_job *job)
+{
+  if (!job) return 0;
+  cmc::SgraModel::Packed pk;
+  const char *err = nullptr;
+  cmc_job k = *job;
+  k.datm = nullptr;
+  if (cmc::SgraModel::host_dims(k, 0, pk, &err)) return 0;
+  const size_t nrep = (size_t)job->nbeta * job->nseq;
+  return grad_extra_offset(pk) + nrep * 3 * (size_t)pk.npts * sizeof(float);
+}
+
+extern "C" int cmc_grad(const cmc_job *job, float *grad, void *stream)
+{
+  cmc::last_error().clear();
+  if (!job) return cmc::fail(CMC_ERR_ARG, "cmc_grad: job is NULL");
+  if (!grad) return cmc::fail(CMC_ERR_ARG, "cmc_grad: grad must be a device pointer");
+  const cmc_job &j = *job;
+  cmc::SgraModel::Packed pk;
+  int rc = grad_dims(j, pk);
+  if (rc) return rc;
+  const size_t need = cmc_grad_work_bytes(job);
+  if (j.work == nullptr || j.work_bytes < need)
+    return cmc::fail(CMC_ERR_ARG, "cmc_grad: job.work is smaller than cmc_grad_work_bytes()");
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = cmc::SgraModel::host_pack(j, pk, j.work, s);
+  if (rc) return cmc::fail(rc, "packing the model data failed");
+  float *gwork = (float *)((unsigned char *)j.work + grad_extra_offset(pk));
+  const int T = 256;
+  const size_t smem = cmc::sgra_grad_smem(j.nptot, T);
+  const unsigned nrep = (unsigned)(j.nbeta * j.nseq);
+  cmc::sgra_grad_kernel<<<nrep, T, smem, s>>>(j, pk, grad, gwork);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CMC_OK : cmc::cuda_fail(e, "sgra_grad_kernel launch");
+}

@@ -58,6 +58,9 @@ struct SgraConsts {
 // Straight-line code: a switched-off component (no inner disk: ai = bi = 0;
 // no Gaussian: zg = 0; sgra_model13 Gaussian-only: ring = 0) contributes
 // zero, so the evaluations of different replicas can be interleaved.
+// Every multiply-add is an explicit fmaf (no a*b + c*d left for the compiler
+// to contract either way), so that the sweep and batch kernels, compiled
+// separately, round identically.
 template <bool BIG = true>
 __device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, const float4 *btab, float u,
                                           float v, float rho)
@@ -68,8 +71,8 @@ __device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, const float4 *bt
   bessel_f12_tab<BIG>(btab, c.kin * rho, g1, g2);
   sincospi_fast(c.dsh * U, &sd, &cd);
   const float rei = c.ai * g1, imi = c.bi * g2 * U;
-  const float re = c.ae * f1 - (rei * cd - imi * sd);
-  const float im = c.be * f2 * U - (rei * sd + imi * cd);
+  const float re = fmaf(c.ae, f1, -fmaf(rei, cd, -(imi * sd)));
+  const float im = fmaf(c.be * f2, U, -fmaf(rei, sd, imi * cd));
   float vre = c.ring ? c.zr * re : 0.0f;
   float vim = c.ring ? c.zr * im : 0.0f;
   const float ug = fmaf(u, c.gc, v * c.gs), vg = fmaf(v, c.gc, -u * c.gs);
@@ -202,8 +205,8 @@ struct SgraModel {
     const float Rin = rq * Rex;
     float d = ecc * (Rex - Rin);
     if (im != 1) d *= cosf(eta - th);
-    const float h = (2.0f / pi) / ((Rex * Rex - Rin * Rin * (1.0f + d / Rex)) * fade
-                                   + (Rex * Rex - Rin * Rin * (1.0f - d / Rex)));
+    const float h = (2.0f / pi) / fmaf(fmaf(-(Rin * Rin), 1.0f + d / Rex, Rex * Rex), fade,
+                                       fmaf(-(Rin * Rin), 1.0f - d / Rex, Rex * Rex));
     const float h0 = fade * h;
     sincosf(th, &c.sth, &c.cth);
     c.kex = 2.0f * pi * Rex;
@@ -294,7 +297,7 @@ struct SgraModel {
         const float2 V = sgra_vis<BIG>(cta.consts[r], btab, d.x, d.y, rho);
         const float n2 = fmaf(V.x, V.x, V.y * V.y);
         const float rs = (n2 > 0.0f) ? rsqrtf(n2) : 0.0f;
-        const float dif = d.z - n2 * rs;
+        const float dif = fmaf(-n2, rs, d.z);
         acc[r] = fmaf(act[r] ? dif * dif : 0.0f, d.w, acc[r]);
         if (PH)
           z[r * npts + i] = (n2 > 0.0f) ? make_float2(V.x * rs, V.y * rs) : make_float2(1.f, 0.f);
@@ -316,13 +319,13 @@ struct SgraModel {
         if (PH) {
           const float2 a = z[r * npts + q.x], b = z[r * npts + q.y], e = z[r * npts + q.z];
           // m = a * b * conj(e): model closure phasor
-          const float abr = a.x * b.x - a.y * b.y, abi = a.x * b.y + a.y * b.x;
-          const float mr = abr * e.x + abi * e.y, mi = abi * e.x - abr * e.y;
+          const float abr = fmaf(a.x, b.x, -(a.y * b.y)), abi = fmaf(a.x, b.y, a.y * b.x);
+          const float mr = fmaf(abr, e.x, abi * e.y), mi = fmaf(abi, e.x, -(abr * e.y));
           // residual phasor e^{i obs} * conj(m)
-          dif = atan2_poly(f.y * mr - f.x * mi, f.x * mr + f.y * mi);
+          dif = atan2_poly(fmaf(f.y, mr, -(f.x * mi)), fmaf(f.x, mr, f.y * mi));
         } else {
           const float x = f.w - (zs[r * npts + q.x] + zs[r * npts + q.y] - zs[r * npts + q.z]);
-          dif = x - 6.2831853071795865f * rintf(x * 0.15915494309189535f);
+          dif = fmaf(-6.2831853071795865f, rintf(x * 0.15915494309189535f), x);
         }
         acc[r] = fmaf(act[r] ? dif * dif : 0.0f, f.z, acc[r]);
       }

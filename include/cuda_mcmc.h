@@ -113,6 +113,18 @@ int cmc_run_noalloc(const cmc_job *job, void *stream);
  * mode 2 = calc_model.  Asynchronous on `stream`. */
 int cmc_eval(const cmc_job *job, int mode, void *stream);
 
+/* ---- chi^2 gradient (Sgr A* model; libcmc_sgra.so only) ---------------------
+ * No counterpart in the reference (its sampler uses no derivatives).
+ * cmc_grad writes chi2c[ist] and d chi2 / d p into grad[ist*nptot + k] at
+ * p = pcur[ist*nptot ..] for every replica ist < nbeta*nseq (zeros where flag
+ * is non-NULL and flag[ist] == 0).  chi2 is the sum the sweep minimises:
+ * amplitude terms, plus closure-phase terms when npass >= 2
+ * (src/gpu_mcmc.cu:305-323 over examples/sgra_model_fit/model.cuh).  Needs
+ * coor, dat, std2r, icoor, idat, pcur, chi2c, status and job->work of at least
+ * cmc_grad_work_bytes(job) bytes; nptot <= 16.  Asynchronous on `stream`. */
+size_t cmc_grad_work_bytes(const cmc_job *job);
+int cmc_grad(const cmc_job *job, float *grad, void *stream);
+
 /* ---- batches of independent jobs (fits) ------------------------------------
  * No counterpart in the reference (it runs one fit per mcmc_cuda call).
  * Every job is a complete cmc_job (device arrays, own sizes; all with the same

@@ -99,6 +99,8 @@ def _declare(L):
     L.or_calc_modchi2.restype = C.c_int
     L.or_calc_model.argtypes = [C.POINTER(_Problem), C.c_int, _fp, _dp, _dp]
     L.or_calc_model.restype = C.c_int
+    L.or_chi2_d.argtypes = [C.POINTER(_Problem), C.c_int, _dp, _dp]
+    L.or_chi2_d.restype = C.c_int
     L.or_sweep.argtypes = [C.POINTER(_Problem), C.POINTER(_SweepState),
                            C.POINTER(_Streams), C.c_int, C.c_int, C.c_int, C.c_int]
     L.or_sweep.restype = C.c_int
@@ -202,6 +204,34 @@ def calc_model(pb: Problem, pcur):
     if rc != OK:
         raise ValueError("or_calc_model failed (%d)" % rc)
     return datm, phase[:, :pb.nvis]
+
+
+def chi2_d(pb: Problem, p):
+    """FP64 chi^2 at FP64 parameters p[..., nptot] (calc_modchi2's terms,
+    src/gpu_mcmc.cu:305-323, without rounding p to float)."""
+    p = np.ascontiguousarray(p, np.float64)
+    shape = p.shape[:-1]
+    p = p.reshape(-1, pb.nptot)
+    out = np.zeros(p.shape[0], np.float64)
+    cp = pb.c()
+    rc = lib().or_chi2_d(C.byref(cp), p.shape[0], _ptr(p, _dp), _ptr(out, _dp))
+    if rc != OK:
+        raise ValueError("or_chi2_d failed (%d)" % rc)
+    return out.reshape(shape)
+
+
+def chi2_grad_fd(pb: Problem, p, h):
+    """Central differences of chi2_d: (chi2(p + h_k e_k) - chi2(p - h_k e_k)) / 2 h_k
+    for every parameter k; p[nrep, nptot], h[nptot] -> [nrep, nptot]."""
+    p = np.asarray(p, np.float64).reshape(-1, pb.nptot)
+    h = np.broadcast_to(np.asarray(h, np.float64), (pb.nptot,))
+    n, k = p.shape
+    pp = np.repeat(p[:, None, :], 2 * k, axis=1)
+    for j in range(k):
+        pp[:, 2 * j, j] += h[j]
+        pp[:, 2 * j + 1, j] -= h[j]
+    c = chi2_d(pb, pp)
+    return (c[:, 0::2] - c[:, 1::2]) / (2.0 * h)
 
 
 @dataclass

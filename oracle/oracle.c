@@ -233,12 +233,10 @@ static double wrap_angle(double x) { return atan2(sin(x), cos(x)); }
  *   iret   : ndat return codes of the pass that produced the term (out)
  * Returns OR_OK or OR_ERR_ARG (unknown sgra imodel).
  */
-static int model_row(const or_problem *pb, const float *p, double *datm,
-                     double *phase, int *iret, int pass_mask)
+static int model_row_d(const or_problem *pb, const double *prm, double *datm,
+                       double *phase, int *iret, int pass_mask)
 {
     int id, j, k, n = pb->nptot;
-    double prm[16];
-    for (j = 0; j < n && j < 16; j++) prm[j] = (double)p[j];
     for (id = 0; id < pb->ndat; id++) iret[id] = 0;
 
     switch (pb->model) {
@@ -327,6 +325,16 @@ static int model_row(const or_problem *pb, const float *p, double *datm,
     }
 }
 
+/* model_row_d at the float parameters the reference's kernels receive. */
+static int model_row(const or_problem *pb, const float *p, double *datm,
+                     double *phase, int *iret, int pass_mask)
+{
+    int j;
+    double prm[16] = {0};
+    for (j = 0; j < pb->nptot && j < 16; j++) prm[j] = (double)p[j];
+    return model_row_d(pb, prm, datm, phase, iret, pass_mask);
+}
+
 static int pass_mask_for(const or_problem *pb)
 {
     return pb->npass >= 2 ? 3 : 1;
@@ -393,6 +401,33 @@ int or_calc_model(const or_problem *pb, int nrep, const float *pcur,
     }
     free(iret);
     return OR_OK;
+}
+
+/*
+ * chi^2 at FP64 parameters p[nrep][nptot] (no rounding of p to float): the
+ * function whose central differences check the gradient.  Same terms as
+ * or_calc_modchi2 (src/gpu_mcmc.cu:305-323).
+ */
+int or_chi2_d(const or_problem *pb, int nrep, const double *p, double *chi2c)
+{
+    int r, rc, nvis = (pb->model == OR_MODEL_SGRA) ? pb->idat[0] : 0;
+    size_t nd = (size_t)(pb->ndat > 0 ? pb->ndat : 1);
+    int *iret = (int *)malloc(sizeof(int) * nd);
+    double *datm = (double *)malloc(sizeof(double) * nd);
+    double *row = (double *)malloc(sizeof(double) * nd);
+    double *phase = (double *)malloc(sizeof(double) * (size_t)(nvis > 0 ? nvis : 1));
+    double prm[16];
+    rc = OR_OK;
+    if (!iret || !datm || !row || !phase || pb->nptot > 16) rc = OR_ERR_ARG;
+    for (r = 0; r < nrep && rc == OR_OK; r++) {
+        int j;
+        for (j = 0; j < pb->nptot; j++) prm[j] = p[(size_t)r * pb->nptot + j];
+        for (j = 0; j < pb->ndat; j++) row[j] = 0.0;
+        rc = model_row_d(pb, prm, datm, phase, iret, pass_mask_for(pb));
+        if (rc == OR_OK) chi2c[r] = chi2_row(pb, datm, iret, row);
+    }
+    free(iret); free(datm); free(row); free(phase);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------ */
