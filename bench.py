@@ -55,9 +55,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="use the library's heuristic shape")
-    ap.add_argument("--workload", default="sgra", choices=["sgra", "batch"],
-                    help="sgra: one 64x32 Sgr A* fit; batch: many independent fits")
+    ap.add_argument("--workload", default="sgra", choices=["sgra", "batch", "ess"],
+                    help="sgra: one 64x32 Sgr A* fit; batch: many independent fits; "
+                         "ess: ESS/sec of Fisher block proposals vs the reference's proposals")
     ap.add_argument("--nfits", type=int, default=1024)
+    ap.add_argument("--ess-burn", type=int, default=2000)
+    ap.add_argument("--ess-iter", type=int, default=4000)
     return ap.parse_args()
 
 
@@ -456,11 +459,80 @@ def run_batch(args, rank, world, local):
     print(json.dumps(line))
 
 
+def run_ess(args, rank, world, local):
+    """ESS per second at the T = 1 slot: the reference's one-parameter
+    proposals (burn-in + recorded iterations) against the Fisher schedule
+    (half the burn-in with those proposals, then Fisher block proposals), same
+    data, replicas and iteration budget.  Posterior accuracy is matched by
+    comparing both posteriors' means and widths with a long Fisher run."""
+    import torch
+    from cuda_mcmc_gb300 import fit, synth
+    from cuda_mcmc_gb300.device import DeviceJob
+    from cuda_mcmc_gb300.ess import ess_per_param
+    from cuda_mcmc_gb300.grad import SgraChi2
+    nseq, nbeta = args.nseq // 2, args.nbeta
+    w = synth.sgra(nvis=args.nvis, ncph=args.ncph, seed=3, nseq=nseq, nbeta=nbeta)
+    obj = SgraChi2.from_workload(w)
+    nb, ni = args.ess_burn, args.ess_iter
+
+    def one(kind, seed, nburn, niter):
+        job = DeviceJob.from_workload(w, niter_total=niter, seed=seed)
+        if not args.no_tune:
+            job.autotune()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if kind == "plain":
+            fit.run_plain(job, nburn, niter)
+        else:
+            fit.run_fisher(job, obj, nburn, niter)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        job.check()
+        pout = job.t["pout"].cpu().numpy()
+        return dt, pout
+
+    one("plain", 5, 20, 20)            # warm-up: library load, autotune cache
+    one("fisher", 5, 20, 20)
+    with Clocks(local) as clk:
+        tp, pp = one("plain", 11, nb, ni)
+        tf, pf = one("fisher", 11, nb, ni)
+    _, pl = one("fisher", 99, nb, 4 * ni)
+    if rank != 0:
+        return
+    sp, sf, sl = (fit.posterior_summary(x) for x in (pp, pf, pl))
+    ess_p, ess_f = ess_per_param(pp), ess_per_param(pf)
+    zp = np.abs(sp["mean"] - sl["mean"]) / np.sqrt(sp["mcse"] ** 2 + sl["mcse"] ** 2)
+    zf = np.abs(sf["mean"] - sl["mean"]) / np.sqrt(sf["mcse"] ** 2 + sl["mcse"] ** 2)
+    line = {
+        "metric": "ESS/sec (min over parameters, T=1 slot, pooled sequences)",
+        "value": float(ess_f.min() / tf), "unit": "ESS/s", "n_gpus": world,
+        "steps": 1, "warmup": 1, "ms_per_step": 1e3 * tf, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "sgra9 %dvis+%dcph, %dx%d replicas" % (w.nvis, w.ndat - w.nvis,
+                                                                       nseq, nbeta),
+                   "budget": "%d burn-in + %d recorded iterations (9 proposals each)" % (nb, ni),
+                   "fisher": "half the burn-in with one-parameter proposals, then block "
+                             "proposals along the Fisher information of each sequence's best "
+                             "replica (adjoint-gradient Hessian)"},
+        "plain": {"value": float(ess_p.min() / tp), "s": tp, "ess": ess_p.tolist()},
+        "fisher": {"value": float(ess_f.min() / tf), "s": tf, "ess": ess_f.tolist()},
+        "speedup": float((ess_f.min() / tf) / (ess_p.min() / tp)),
+        "accuracy": {"z_mean_plain_vs_long": zp.tolist(), "z_mean_fisher_vs_long": zf.tolist(),
+                     "sd_ratio_plain": (sp["sd"] / sl["sd"]).tolist(),
+                     "sd_ratio_fisher": (sf["sd"] / sl["sd"]).tolist(),
+                     "long_run": "Fisher schedule, %d recorded iterations" % (4 * ni)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args)
     if args.impl == "mine" and args.workload == "batch":
         run_batch(args, rank, world, local)
+    elif args.impl == "mine" and args.workload == "ess":
+        run_ess(args, rank, world, local)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -17,6 +17,7 @@ _lock = threading.Lock()
 CMC_OK, CMC_ERR_ARG, CMC_ERR_CUDA, CMC_ERR_STREAM, CMC_ERR_MODEL, CMC_ERR_NOMEM, \
     CMC_ERR_UNSUPPORTED = range(7)
 CMC_RNG_CURAND, CMC_RNG_INJECTED = 0, 1
+CMC_PROP_SINGLE, CMC_PROP_BLOCK = 0, 1
 MODE_MODCHI2, MODE_MODEL = 1, 2
 
 
@@ -51,6 +52,7 @@ class CmcJob(C.Structure):
         ("inj_cur", _vp),
         ("work", _vp), ("work_bytes", C.c_size_t),
         ("status", _vp),
+        ("prop_mode", C.c_int), ("prop_reserved", C.c_int), ("prop_chol", _vp),
     ]
 
 

@@ -97,7 +97,7 @@ __host__ __device__ inline unsigned align16(unsigned x) { return (x + 15u) & ~15
 // host and carves the buffer on the device.  `hist` holds the burn-in
 // accept/reject history n_hist as one bit per entry: [R][nprm][hist_words(nadj)].
 struct SmemPlan {
-  unsigned params, plast, ptmp, rf, ri, sf, si, hist, tab, consts, red, xch, stage,
+  unsigned params, plast, ptmp, blk, rf, ri, sf, si, hist, tab, consts, red, xch, stage,
       scratch, total;
 };
 
@@ -112,6 +112,7 @@ __host__ __device__ inline SmemPlan make_plan(int R, int nthreads, int nptot, in
   p.params = o;  o = align16(o + 4u * R * nptot);
   p.plast = o;   o = align16(o + 4u * R * nptot);
   p.ptmp = o;    o = align16(o + 4u * (R * nptot + R));
+  p.blk = o;     o = align16(o + 4u * R * nptot);
   p.rf = o;      o = align16(o + 4u * R * kRepF);
   p.ri = o;      o = align16(o + 4u * R * kRepI);
   p.sf = o;      o = align16(o + 4u * R * nprm);

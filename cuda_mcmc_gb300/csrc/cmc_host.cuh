@@ -188,6 +188,10 @@ inline int validate_common(const cmc_job &j, int mode)
       return fail(CMC_ERR_ARG, "rndst is required for the cuRAND generator");
     if (j.rng_mode == CMC_RNG_INJECTED && (!j.inj_u || !j.inj_n || !j.inj_cur))
       return fail(CMC_ERR_ARG, "injected streams need inj_u, inj_n and inj_cur");
+    if (j.prop_mode != CMC_PROP_SINGLE && j.prop_mode != CMC_PROP_BLOCK)
+      return fail(CMC_ERR_ARG, "prop_mode must be CMC_PROP_SINGLE (0) or CMC_PROP_BLOCK (1)");
+    if (j.prop_mode == CMC_PROP_BLOCK && !j.prop_chol)
+      return fail(CMC_ERR_ARG, "block proposals need prop_chol [nseq][nprm][nprm]");
   }
   return CMC_OK;
 }

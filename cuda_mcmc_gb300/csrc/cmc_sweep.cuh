@@ -29,6 +29,8 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   float *params = (float *)(smem + P.params);   // [R][nptot]
   float *plast = (float *)(smem + P.plast);     // [R][nptot] params of last evaluation
   float *ptmp = (float *)(smem + P.ptmp);       // [R][nptot] + [R] exchange staging
+  float *blk = (float *)(smem + P.blk);         // [R][nptot] block mode: pre-proposal params
+  const bool block = (job.prop_mode == CMC_PROP_BLOCK);
   float *rf = (float *)(smem + P.rf);
   int *ri = (int *)(smem + P.ri);
   float *s_ptent = rf, *s_chi2c = rf + R, *s_chi2n = rf + 2 * R, *s_beta = rf + 3 * R;
@@ -187,7 +189,10 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
         s_chi2c[r] = c2;
         s_nacpt[r * nprm + k] += 1;
       } else {
-        params[r * nptot + s_ptentn[r]] = s_ptent[r];
+        if (block)
+          for (int j = 0; j < nptot; ++j) params[r * nptot + j] = blk[r * nptot + j];
+        else
+          params[r * nptot + s_ptentn[r]] = s_ptent[r];
         s_flag[r] = 0;
       }
     }
@@ -216,6 +221,43 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
     }
   };
 
+  // Block proposal for local replica r (thread r): all nprm parameters move,
+  // p_ivar[i] += pstp[0] * (L z)_i with z ~ N(0, I) drawn in order z_0..z_{nprm-1}
+  // and (L z)_i accumulated over j = 0..i by fmaf.  A proposal outside the
+  // prior box is rejected without evaluation (as in gen_proposal); the
+  // pre-proposal parameters stay in blk for the rejection path.
+  auto block_proposal = [&](int r) {
+    const float *L = job.prop_chol + (size_t)iseq * nprm * nprm;
+    float *acc = ptmp + r * nptot;
+    for (int j = 0; j < nptot; ++j) blk[r * nptot + j] = params[r * nptot + j];
+    for (int i = 0; i < nprm; ++i) acc[i] = 0.0f;
+    for (int j = 0; j < nprm; ++j) {
+      const float z = rng.normal();
+      for (int i = j; i < nprm; ++i) acc[i] = __fmaf_rn(__ldg(&L[i * nprm + j]), z, acc[i]);
+    }
+    const float sd = s_pstp[r * nprm];
+    bool out = false;
+    for (int i = 0; i < nprm; ++i) {
+      const int t = s_ivar[i];
+      float p = __fmaf_rn(sd, acc[i], blk[r * nptot + t]);
+      if (s_pdescr[t] == 2) p = atan2f(sinf(p), cosf(p));
+      out |= (p < s_pmin[t]) || (p > s_pmax[t]);
+      params[r * nptot + t] = p;
+    }
+    s_k[r] = 0;
+    s_ptentn[r] = s_ivar[0];
+    s_ptent[r] = blk[r * nptot + s_ivar[0]];
+    if (out) {
+      for (int j = 0; j < nptot; ++j) params[r * nptot + j] = blk[r * nptot + j];
+      s_flag[r] = 0;
+    } else {
+      s_flag[r] = 1;
+      for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
+      Model::prepare(cta, r, &params[r * nptot]);
+      s_evald[r] = 1;
+    }
+  };
+
   const int nsteps = job.nburn + job.niter;
   for (int step = 0; step < nsteps; ++step) {
     const bool burn = step < job.nburn;
@@ -223,25 +265,29 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
       if (tid < R) {
         const int r = tid;
         if (ipm > 0) accept_adjust(r, burn);
-        // gen_proposal (src/gpu_mcmc.cu:361-411)
-        const int k = rng.index(nprm, job.status);
-        const int t = s_ivar[k];
-        float p = params[r * nptot + t];
-        s_k[r] = k;
-        s_ptentn[r] = t;
-        s_ptent[r] = p;
-        const float sd = s_pstp[r * nprm + k];
-        const float rn = rng.normal();
-        p = __fmaf_rn(sd, rn, p);
-        if (s_pdescr[t] == 2) p = atan2f(sinf(p), cosf(p));
-        if ((p < s_pmin[t]) || (p > s_pmax[t])) {
-          s_flag[r] = 0;
+        if (block) {
+          block_proposal(r);
         } else {
-          s_flag[r] = 1;
-          params[r * nptot + t] = p;
-          for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
-          Model::prepare(cta, r, &params[r * nptot]);
-          s_evald[r] = 1;
+          // gen_proposal (src/gpu_mcmc.cu:361-411)
+          const int k = rng.index(nprm, job.status);
+          const int t = s_ivar[k];
+          float p = params[r * nptot + t];
+          s_k[r] = k;
+          s_ptentn[r] = t;
+          s_ptent[r] = p;
+          const float sd = s_pstp[r * nprm + k];
+          const float rn = rng.normal();
+          p = __fmaf_rn(sd, rn, p);
+          if (s_pdescr[t] == 2) p = atan2f(sinf(p), cosf(p));
+          if ((p < s_pmin[t]) || (p > s_pmax[t])) {
+            s_flag[r] = 0;
+          } else {
+            s_flag[r] = 1;
+            params[r * nptot + t] = p;
+            for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
+            Model::prepare(cta, r, &params[r * nptot]);
+            s_evald[r] = 1;
+          }
         }
       }
       __syncthreads();

@@ -64,8 +64,9 @@ __device__ __forceinline__ float atan2_poly(float y, float x)
   float p = kAtanP[9];
 #pragma unroll
   for (int k = 8; k >= 0; --k) p = fmaf(p, s, kAtanP[k]);
-  float r = p * a;
-  if (ay > ax) r = 1.57079632679489662f - r;
+  // pi/2 - p a as an explicit fmaf: no multiply-add is left for the compiler
+  // to contract differently in different kernels
+  float r = (ay > ax) ? fmaf(-p, a, 1.57079632679489662f) : p * a;
   if (x < 0.0f) r = 3.14159265358979324f - r;
   return copysignf(r, y);
 }

@@ -233,6 +233,43 @@ class DeviceJob:
             src = torch.as_tensor(np.ascontiguousarray(v)).to(dtype=dst.dtype).reshape(dst.shape)
             dst.copy_(src.to(self.device))
 
+    # ---- proposals ---------------------------------------------------------------
+    def set_block_proposals(self, chol, scale=None):
+        """Switch to block proposals p += pstp[0] * L z for all nprm parameters
+        at once.  ``chol`` [nseq, nprm, nprm] (or [nprm, nprm] for every
+        sequence): lower Cholesky factors of the beta = 1 proposal covariance
+        in ivar order.  ``scale`` [nbeta, nseq] (default 1/sqrt(beta), the
+        tempered target's width) becomes pstp[0], the per-replica step that
+        burn-in keeps adapting.  The acceptance counters of slot 0 restart."""
+        chol = np.asarray(chol, np.float32)
+        if chol.ndim == 2:
+            chol = np.broadcast_to(chol, (self.nseq,) + chol.shape)
+        if chol.shape != (self.nseq, self.nprm, self.nprm):
+            raise ValueError("chol must be [nseq, nprm, nprm] = [%d, %d, %d]"
+                             % (self.nseq, self.nprm, self.nprm))
+        self.t["prop_chol"] = _dev(np.tril(chol), _F32, self.device)
+        beta = self.t["beta"].double()
+        if scale is None:
+            scale = (1.0 / torch.sqrt(beta))[:, None].expand(self.nbeta, self.nseq)
+        scale = torch.as_tensor(np.asarray(scale, np.float32) if not torch.is_tensor(scale)
+                                else scale).to(self.device, _F32).reshape(self.nbeta, self.nseq)
+        self.t["pstp"][0].copy_(scale)
+        self.t["n_cnt"][0].fill_(1)
+        self.t["n_acpt"][0].zero_()
+        self.t["n_hist"][:, 0].zero_()
+        self.job.prop_chol = _ptr(self.t["prop_chol"])
+        self.job.prop_mode = _lib.CMC_PROP_BLOCK
+
+    def set_single_proposals(self, pstp0=None):
+        """Back to the reference's one-parameter proposals; ``pstp0`` [nbeta,
+        nseq] restores parameter 0's step (block mode used pstp[0] as its
+        scale)."""
+        self.job.prop_mode = _lib.CMC_PROP_SINGLE
+        self.job.prop_chol = None
+        if pstp0 is not None:
+            self.t["pstp"][0].copy_(torch.as_tensor(np.asarray(pstp0, np.float32)).to(self.device)
+                                    .reshape(self.nbeta, self.nseq))
+
 
 class BatchJob:
     """Many independent fits of one model (DeviceJobs with the same nbeta) run

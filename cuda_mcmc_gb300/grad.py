@@ -116,28 +116,43 @@ def fisher(obj: SgraChi2, p, ivar=None, beta=1.0, rel_step=1e-3, scale=None, flo
     parameters ``ivar`` (default: all), for the tempered target
     exp(-beta chi^2 / 2).  Row k is the central difference of the adjoint
     gradient along parameter ivar[k] with step rel_step * scale[k]
-    (scale: the prior widths, default max(|p_k|, 1)); the result is
+    (scale: e.g. the prior widths, default max(|p_k|, 1)); the result is
     symmetrised and its eigenvalues raised to ``floor`` (default 1e-9 of the
     largest), so that it inverts to a covariance.  Returns float64 [k, k]."""
-    p = np.asarray(p, np.float64).ravel()
-    ivar = np.arange(p.size) if ivar is None else np.asarray(ivar, np.int64)
+    return fisher_many(obj, np.asarray(p, np.float64).reshape(1, -1), ivar, beta, rel_step,
+                       scale, floor)[0]
+
+
+def fisher_many(obj: SgraChi2, P, ivar=None, beta=1.0, rel_step=1e-3, scale=None, floor=None):
+    """:func:`fisher` at every row of P [m, nptot] with one adjoint call
+    (2 k m displaced parameter rows).  Returns float64 [m, k, k]."""
+    P = np.asarray(P, np.float64)
+    m, nptot = P.shape
+    ivar = np.arange(nptot) if ivar is None else np.asarray(ivar, np.int64)
     k = ivar.size
-    sc = np.maximum(np.abs(p[ivar]), 1.0) if scale is None else np.asarray(scale, np.float64)
-    h = rel_step * sc
-    P = np.repeat(p[None, :], 2 * k, axis=0)
-    for a, iv in enumerate(ivar):
-        P[2 * a, iv] += h[a]
-        P[2 * a + 1, iv] -= h[a]
-    hp = (P.astype(np.float32).astype(np.float64) - p[None, :])   # steps actually taken
-    _, g = obj(P.astype(np.float32))
-    g = g.double().cpu().numpy()[:, ivar]
-    step = hp[0::2, ivar].diagonal() - hp[1::2, ivar].diagonal()
-    H = (g[0::2] - g[1::2]) / step[:, None]
-    H = 0.5 * (H + H.T) * (0.5 * beta)
-    w, V = np.linalg.eigh(H)
-    fl = (1e-9 * max(float(w.max()), 0.0) if floor is None else float(floor))
-    w = np.maximum(w, max(fl, np.finfo(np.float64).tiny))
-    return (V * w) @ V.T
+    if scale is None:
+        sc = np.maximum(np.abs(P[:, ivar]), 1.0)
+    else:   # per parameter: [nptot] (read at ivar) or [k]
+        sc = np.asarray(scale, np.float64).ravel()
+        sc = np.broadcast_to(sc[ivar] if sc.size == nptot else sc, (m, k))
+    h = rel_step * sc                                           # [m, k]
+    Q = np.repeat(P[:, None, :], 2 * k, axis=1)                 # [m, 2k, nptot]
+    a = np.arange(k)
+    Q[:, 2 * a, ivar] += h
+    Q[:, 2 * a + 1, ivar] -= h
+    Q32 = Q.astype(np.float32)
+    taken = Q32[:, 2 * a, ivar].astype(np.float64) - Q32[:, 2 * a + 1, ivar].astype(np.float64)
+    _, g = obj(Q32.reshape(m * 2 * k, nptot))
+    g = g.double().cpu().numpy().reshape(m, 2 * k, nptot)[:, :, ivar]
+    H = (g[:, 0::2] - g[:, 1::2]) / taken[:, :, None]          # [m, k, k]
+    H = 0.5 * (H + np.swapaxes(H, 1, 2)) * (0.5 * beta)
+    out = np.empty_like(H)
+    for i in range(m):
+        w, V = np.linalg.eigh(H[i])
+        fl = (1e-9 * max(float(w.max()), 0.0) if floor is None else float(floor))
+        w = np.maximum(w, max(fl, np.finfo(np.float64).tiny))
+        out[i] = (V * w) @ V.T
+    return out
 
 
 def proposal_cholesky(F, d=None):

@@ -21,6 +21,16 @@ enum cmc_status {
   CMC_ERR_UNSUPPORTED = 6 /* no kernel configuration fits these sizes         */
 };
 
+enum cmc_prop_mode {
+  CMC_PROP_SINGLE = 0,    /* the reference's proposals: one parameter k drawn
+                             per proposal, p_k += pstp[k] * N(0,1)
+                             (src/gpu_mcmc.cu:361-411)                        */
+  CMC_PROP_BLOCK = 1      /* no counterpart in the reference: all nprm
+                             parameters at once, p += pstp[0] * L z with
+                             z ~ N(0, I) and L = prop_chol[iseq]; acceptance
+                             bookkeeping and step adaptation on slot k = 0    */
+};
+
 enum cmc_rng_mode {
   CMC_RNG_CURAND = 0,     /* cuRAND XORWOW, curand_init(seed, ist, 0): the
                              reference's generator (src/gpu_mcmc.cu:228-239)  */
@@ -82,6 +92,15 @@ typedef struct cmc_job {
 
   /* device status word (CMC_* code), written by the kernels */
   int *status;
+
+  /* proposal kind (enum cmc_prop_mode) and, for CMC_PROP_BLOCK, the lower
+     Cholesky factors of the proposal covariance of each sequence in ivar
+     order: prop_chol[(iseq*nprm + i)*nprm + j], j <= i (the upper triangle is
+     not read).  Typically (2.38^2/nprm) F^-1 for the Fisher information F of
+     the beta = 1 target; replica ibeta scales it by pstp[0][ibeta][iseq]. */
+  int prop_mode;
+  int prop_reserved;
+  const float *prop_chol;
 } cmc_job;
 
 #ifdef __cplusplus

@@ -89,7 +89,8 @@ class _SweepState(C.Structure):
                 ("pout", _fp), ("tout", _ip), ("chi2", _fp),
                 ("datm", _dp), ("chi2m", _dp),
                 ("tr_dec", _bp), ("tr_margin", _dp), ("tr_xk", _bp),
-                ("tr_xdec", _bp), ("tr_xmargin", _dp)]
+                ("tr_xdec", _bp), ("tr_xmargin", _dp),
+                ("prop_mode", C.c_int), ("prop_chol", _fp)]
 
 
 def _declare(L):
@@ -352,8 +353,10 @@ class Trace:
 
 
 def sweep(pb: Problem, st: SweepState, rs: Streams, do_init, nburn, niter, itr0=0,
-          trace=False):
-    """Run the restated sweep in place on ``st``; returns a Trace or None."""
+          trace=False, prop_chol=None):
+    """Run the restated sweep in place on ``st``; returns a Trace or None.
+    ``prop_chol`` [nseq, nprm, nprm] switches to the library's block
+    proposals (lower Cholesky factor per sequence, scaled by pstp[0])."""
     nrep = st.nbeta * st.nseq
     nstep = nburn + niter
     tr = None
@@ -367,6 +370,9 @@ def sweep(pb: Problem, st: SweepState, rs: Streams, do_init, nburn, niter, itr0=
                  "n_hist", "tcur", "pout", "tout", "chi2"):
         assert getattr(st, name).flags["C_CONTIGUOUS"], name
     st.chi2c = np.ascontiguousarray(st.chi2c, np.float64)
+    chol = None if prop_chol is None else np.ascontiguousarray(prop_chol, np.float32)
+    if chol is not None and chol.shape != (st.nseq, st.nprm, st.nprm):
+        raise ValueError("prop_chol must be [nseq, nprm, nprm]")
     cst = _SweepState(
         st.nprm, int(st.n_hist.shape[0]), st.nbeta, st.nseq, int(st.pout.shape[-1]),
         _ptr(st.pdescr, _ip), _ptr(st.ivar, _ip), _ptr(st.invar, _ip),
@@ -378,7 +384,8 @@ def sweep(pb: Problem, st: SweepState, rs: Streams, do_init, nburn, niter, itr0=
         _ptr(st.datm, _dp), _ptr(st.chi2m, _dp),
         _ptr(tr.dec if tr else None, _bp), _ptr(tr.margin if tr else None, _dp),
         _ptr(tr.xk if tr else None, _bp), _ptr(tr.xdec if tr else None, _bp),
-        _ptr(tr.xmargin if tr else None, _dp))
+        _ptr(tr.xmargin if tr else None, _dp),
+        0 if prop_chol is None else 1, _ptr(chol, _fp))
     cs = _Streams(_ptr(rs.u, _fp), _ptr(rs.n, _fp), rs.u.shape[1], rs.n.shape[1],
                   _ptr(rs.cu, _ip), _ptr(rs.cn, _ip), 0)
     cp = pb.c()

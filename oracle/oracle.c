@@ -495,6 +495,13 @@ typedef struct {
     signed char *tr_xk;    /* [nstep][nseq][nbeta]: pair index k */
     signed char *tr_xdec;  /* [nstep][nseq][nbeta]: swapped? */
     double *tr_xmargin;    /* [nstep][nseq][nbeta]: u - alpha */
+    /* proposal kind: 0 = the reference's one-parameter proposals; 1 = block
+       proposals p_ivar[i] += pstp[0] * (L z)_i, L = prop_chol[iseq] (lower,
+       row-major [nprm][nprm]), z ~ N(0, I) drawn z_0..z_{nprm-1}, (L z)_i
+       accumulated over j = 0..i with fmaf; bookkeeping on slot k = 0.  This
+       mode is the library's extension, restated here as its checker. */
+    int prop_mode;
+    const float *prop_chol;  /* [nseq][nprm][nprm] */
 } or_sweep_state;
 
 static int chi2_of(const or_problem *pb, const float *p, double *datm_row,
@@ -520,9 +527,11 @@ int or_sweep(const or_problem *pb, or_sweep_state *st, or_streams *rs,
     int ist, i, k, t, step, itr, ipm, rc = OR_OK;
     double *datm_tmp, *chi2m_tmp, *phase_tmp;
     int *iret;
+    float bk[64];   /* block mode: the pre-proposal parameters */
 
     if (nbeta < 2 || nseq < 1 || nprm < 1 || nptot < nprm || st->nadj < 1)
         return OR_ERR_ARG;
+    if (st->prop_mode == 1 && (!st->prop_chol || nptot > 64)) return OR_ERR_ARG;
     datm_tmp = (double *)calloc((size_t)nrep * (ndat > 0 ? ndat : 1), sizeof(double));
     chi2m_tmp = (double *)calloc((size_t)nrep * (ndat > 0 ? ndat : 1), sizeof(double));
     phase_tmp = (double *)calloc((size_t)(nvis > 0 ? nvis : 1), sizeof(double));
@@ -560,6 +569,38 @@ int or_sweep(const or_problem *pb, or_sweep_state *st, or_streams *rs,
                 int ibeta = ist / nseq, iseq = ist % nseq, kk, pt, ip;
                 float r, p, sd, rn;
                 size_t tix = ((size_t)step * nprm + ipm) * nrep + ist;
+                if (st->prop_mode == 1) {
+                    const float *L = st->prop_chol + (size_t)iseq * nprm * nprm;
+                    float acc[64], zj, sdb;
+                    int out = 0, j2;
+                    if (nprm > 64) { rc = OR_ERR_ARG; goto done; }
+                    for (i = 0; i < nprm; i++) acc[i] = 0.0f;
+                    for (j2 = 0; j2 < nprm; j2++) {
+                        zj = draw_n(rs, ist);
+                        for (i = j2; i < nprm; i++) acc[i] = fmaf(L[i * nprm + j2], zj, acc[i]);
+                    }
+                    if (rs->overflow) { rc = OR_ERR_STREAM; goto done; }
+                    for (i = 0; i < nptot; i++) bk[i] = st->pcur[(size_t)ist * nptot + i];
+                    sdb = st->pstp[(size_t)ibeta * nseq + iseq];     /* slot k = 0 */
+                    for (i = 0; i < nprm; i++) {
+                        int tt = st->ivar[i];
+                        float pp = fmaf(sdb, acc[i], bk[tt]);
+                        if (st->pdescr[tt] == 2) pp = wrap_angle_f(pp);
+                        if (pp < st->pmint[tt] || pp > st->pmaxt[tt]) out = 1;
+                        st->pcur[(size_t)ist * nptot + tt] = pp;
+                    }
+                    t = st->ivar[0];
+                    st->ptentn[ist] = t;
+                    st->ptent[ist] = bk[t];
+                    if (out) {
+                        for (i = 0; i < nptot; i++) st->pcur[(size_t)ist * nptot + i] = bk[i];
+                        st->flag[ist] = 0;
+                    } else {
+                        st->flag[ist] = 1;
+                    }
+                    pt = ist * nptot + t;
+                    goto evaluate;
+                }
                 /* gen_proposal, gpu_mcmc.cu:361-411 */
                 do {
                     r = draw_u(rs, ist);
@@ -581,6 +622,7 @@ int or_sweep(const or_problem *pb, or_sweep_state *st, or_streams *rs,
                     st->flag[ist] = 1;
                     st->pcur[pt] = p;
                 }
+            evaluate:
                 /* calc_chi2_terms + spmp_mcmc, gpu_mcmc.cu:273-325, 426-474 */
                 if (st->flag[ist] != 0) {
                     double c2, a, alpha;
@@ -598,7 +640,10 @@ int or_sweep(const or_problem *pb, or_sweep_state *st, or_streams *rs,
                         st->n_acpt[(nbeta * st->invar[t] + ibeta) * nseq + iseq]++;
                         if (st->tr_dec) st->tr_dec[tix] = 1;
                     } else {
-                        st->pcur[pt] = st->ptent[ist];
+                        if (st->prop_mode == 1)
+                            for (i = 0; i < nptot; i++) st->pcur[(size_t)ist * nptot + i] = bk[i];
+                        else
+                            st->pcur[pt] = st->ptent[ist];
                         st->flag[ist] = 0;
                         if (st->tr_dec) st->tr_dec[tix] = 0;
                     }

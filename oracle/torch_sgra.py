@@ -61,15 +61,23 @@ def j1(x):
     return _J1.apply(x)
 
 
+def _j2(x):
+    """J2(x) = 2 J1(x)/x - J0(x), with its series x^2/8 near 0 (no 0/0, so
+    that autograd stays finite at x = 0, e.g. Rin = 0)."""
+    small = x.abs() < 1e-4
+    xs = torch.where(small, torch.ones_like(x), x)
+    return torch.where(small, x * x / 8.0, 2.0 * j1(xs) / xs - j0(xs))
+
+
 def _ring(prm, U, rho, Rex, Rin, rq, d, h, h0):
     """Crescent (outer disk minus shifted inner disk), rho > 1e-7."""
     pi = math.pi
     aRex = 2.0 * pi * rho * Rex
     ree = 0.5 * (h + h0) * Rex * j1(aRex) / rho
-    j2e = 2.0 * j1(aRex) / aRex - j0(aRex)
+    j2e = _j2(aRex)
     ime = (h - h0) / (4 * pi) * (pi * Rex * (j0(aRex) - j2e) / rho ** 2 - j1(aRex) / rho ** 3) * U
     aRin = 2.0 * pi * rho * Rin
-    j2i = 2.0 * j1(aRin) / aRin - j0(aRin)
+    j2i = _j2(aRin)
     rei = 0.5 * (h + h0 - d * (h - h0) / Rex) * Rin * j1(aRin) / rho
     imi = (h - h0) / (4 * pi) * rq * (pi * Rin * (j0(aRin) - j2i) / rho ** 2
                                       - j1(aRin) / rho ** 3) * U
@@ -79,9 +87,9 @@ def _ring(prm, U, rho, Rex, Rin, rq, d, h, h0):
 
 def vis(prm, u, v, imodel=1):
     """Complex visibility (re, im) of parameter rows prm[n, nptot] at the uv
-    points u[m], v[m] -> two [n, m] tensors.  Needs Rin != 0 and the Gaussian
-    switched on (gax, aq, gq != 0, gq != 1 for sgra_model13), the region the
-    gradient tests sample."""
+    points u[m], v[m] -> two [n, m] tensors.  Needs the Gaussian switched on
+    (gax, aq, gq != 0, gq != 1 for sgra_model13), the region the gradient
+    tests sample."""
     pi = math.pi
     P = [prm[:, k:k + 1] for k in range(prm.shape[1])]
     u, v = u[None, :], v[None, :]

@@ -1,0 +1,135 @@
+"""Block proposals (CMC_PROP_BLOCK): every parameter moves at once along a
+caller-given Cholesky factor.  The oracle's sweep restates the mode; from the
+same state and injected draws the kernel makes the oracle's decisions
+iteration by iteration (near ties excepted, as in the single-parameter
+lock-step test), and the batch path runs the same chains as single launches.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cuda_mcmc_gb300 import _lib, synth
+from cuda_mcmc_gb300.device import BatchJob, DeviceJob
+
+pytestmark = pytest.mark.gpu
+
+CHI2_RTOL, TIE_RTOL = 1e-5, 1e-3
+
+
+def _pb(w):
+    return oracle.Problem(w.model, w.coor, w.dat, w.std2r, w.icoor, w.idat, w.nptot, w.imodel,
+                          w.npass)
+
+
+def _chol(w, nseq, seed, frac=0.02):
+    """Seeded lower-triangular factors with prior-width-scaled diagonals."""
+    rng = np.random.default_rng(seed)
+    ivar = np.where(np.asarray(w.pdescr) != 0)[0]
+    width = (w.pmaxt - w.pmint)[ivar].astype(np.float64)
+    k = ivar.size
+    out = np.empty((nseq, k, k), np.float32)
+    for q in range(nseq):
+        A = rng.standard_normal((k, k)) * 0.3 + np.eye(k)
+        C = (A @ A.T) * np.outer(width, width) * frac ** 2
+        out[q] = np.linalg.cholesky(C).astype(np.float32)
+    return out
+
+
+def _oracle_state_from(s, w, niter_total):
+    st = oracle.new_state(w.pdescr, w.pmint, w.pmaxt, w.beta(), w.nseq, niter_total,
+                          ptotal=w.ptotal, ndat=w.ndat)
+    for f in ("pcur", "flag", "ptent", "ptentn", "pstp", "n_acpt", "n_exch", "n_cnt", "n_hist",
+              "tcur"):
+        getattr(st, f)[...] = s[f]
+    st.chi2c = s["chi2c"].astype(np.float64)
+    return st
+
+
+@pytest.mark.parametrize("cfg", ["sgra", "rosenbrock"])
+def test_block_proposals_lockstep_vs_oracle(cfg):
+    if cfg == "sgra":
+        w = synth.sgra(nvis=400, ncph=120, seed=8, nseq=2, nbeta=8)
+    else:
+        w = synth.rosenbrock(nseq=2, nbeta=8)
+    nburn, niter = 6, 6
+    nrep = w.nbeta * w.nseq
+    rs = oracle.make_streams(nrep, 4000, 4000, 91)
+    job = DeviceJob.from_workload(w, niter_total=niter, rng="injected", streams=(rs.u, rs.n))
+    job.run(0, 0, do_init=True)
+    job.check()
+    L = _chol(w, w.nseq, seed=3)
+    job.set_block_proposals(L)
+    s = job.to_numpy()
+    assert np.allclose(s["pstp"][0], 1.0 / np.sqrt(w.beta())[:, None])
+    mismatched = 0
+    moved = 0
+    for step in range(nburn + niter):
+        burn = step < nburn
+        st = _oracle_state_from(s, w, niter)
+        p_before = s["pcur"].copy()
+        ors = oracle.Streams(rs.u, rs.n, s["inj_cur"][:, 0].copy(), s["inj_cur"][:, 1].copy())
+        tr = oracle.sweep(_pb(w), st, ors, 0, 1 if burn else 0, 0 if burn else 1, trace=True,
+                          prop_chol=L)
+        job.run(1 if burn else 0, 0 if burn else 1, itr0=0)
+        job.check()
+        s = job.to_numpy()
+        same = (np.array_equal(s["n_acpt"], st.n_acpt) and np.array_equal(s["n_exch"], st.n_exch)
+                and np.array_equal(s["tcur"], st.tcur) and np.array_equal(s["n_hist"], st.n_hist)
+                and np.array_equal(s["inj_cur"], np.stack([ors.cu, ors.cn], 1)))
+        if same:
+            assert np.allclose(s["pcur"], st.pcur, rtol=1e-6, atol=1e-7)
+            assert np.allclose(s["pstp"], st.pstp, rtol=1e-6)
+            assert np.max(np.abs(s["chi2c"] - st.chi2c) / np.maximum(st.chi2c, 1e-6)) < CHI2_RTOL
+        else:
+            alpha_m = np.abs(tr.margin[tr.dec >= 0])
+            x_m = np.abs(tr.xmargin)
+            assert alpha_m.min(initial=1.0) < TIE_RTOL or x_m.min(initial=1.0) < TIE_RTOL
+            mismatched += 1
+        # block moves change several parameters of a replica at once
+        ivar = np.where(np.asarray(w.pdescr) != 0)[0]
+        changed = (s["pcur"][..., ivar] != p_before[..., ivar]).sum(-1)
+        moved += int((changed > 1).sum())
+    assert mismatched <= 1
+    assert moved > 0
+    # only slot 0 of the acceptance bookkeeping is used
+    assert np.all(s["n_acpt"][1:] == 0)
+
+
+def test_block_batch_equals_single_launches():
+    fits = [synth.sgra(nvis=nv, ncph=nc, seed=60 + i, nseq=2, nbeta=8)
+            for i, (nv, nc) in enumerate([(150, 45), (900, 270)])]
+    nburn, niter = 5, 6
+    jobs, refs = [], []
+    for i, w in enumerate(fits):
+        L = _chol(w, w.nseq, seed=10 + i)
+        for lst in (jobs, refs):
+            j = DeviceJob.from_workload(w, niter_total=niter, seed=300 + i)
+            j.run(0, 0, do_init=True)
+            j.set_block_proposals(L)
+            lst.append(j)
+    batch = BatchJob(jobs)
+    classes = batch.classes()
+    batch.run(nburn, 0)
+    batch.run(0, niter)
+    batch.check()
+    for i, w in enumerate(fits):
+        got = jobs[i].to_numpy()
+        ok = False
+        for c in classes:
+            ref = DeviceJob.from_workload(w, niter_total=niter, seed=300 + i)
+            ref.run(0, 0, do_init=True)
+            ref.set_block_proposals(_chol(w, w.nseq, seed=10 + i))
+            ref.shape = {"R": c["R"], "T": c["T"], "phasor": c["phasor"]}
+            try:
+                ref.run(nburn, 0)
+                ref.run(0, niter)
+                ref.check()
+            except _lib.McmcError:
+                continue
+            r = ref.to_numpy()
+            if np.array_equal(r["rndst"], got["rndst"]) and np.array_equal(r["pout"], got["pout"]):
+                for f in ("chi2", "tout", "pcur", "chi2c", "n_acpt", "pstp"):
+                    assert np.array_equal(r[f], got[f]), f
+                ok = True
+                break
+        assert ok, "fit %d matched no class shape" % i
