@@ -55,9 +55,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="use the library's heuristic shape")
-    ap.add_argument("--workload", default="sgra", choices=["sgra", "batch", "ess"],
+    ap.add_argument("--workload", default="sgra", choices=["sgra", "batch", "ess", "ess-batch"],
                     help="sgra: one 64x32 Sgr A* fit; batch: many independent fits; "
-                         "ess: ESS/sec of Fisher block proposals vs the reference's proposals")
+                         "ess: ESS/sec of Fisher block proposals vs the reference's proposals; "
+                         "ess-batch: the same over many fits, batched vs one fit per launch")
     ap.add_argument("--nfits", type=int, default=1024)
     ap.add_argument("--ess-burn", type=int, default=2000)
     ap.add_argument("--ess-iter", type=int, default=4000)
@@ -462,8 +463,7 @@ def run_batch(args, rank, world, local):
 def run_ess(args, rank, world, local):
     """ESS per second at the T = 1 slot: the reference's one-parameter
     proposals (burn-in + recorded iterations) against the Fisher schedule
-    (half the burn-in with those proposals, then Fisher block proposals), same
-    data, replicas and iteration budget.  Posterior accuracy is matched by
+    (fit.run_fisher), same data, replicas and iteration budget.  Posterior accuracy is matched by
     comparing both posteriors' means and widths with a long Fisher run."""
     import torch
     from cuda_mcmc_gb300 import fit, synth
@@ -511,9 +511,10 @@ def run_ess(args, rank, world, local):
         "config": {"workload": "sgra9 %dvis+%dcph, %dx%d replicas" % (w.nvis, w.ndat - w.nvis,
                                                                        nseq, nbeta),
                    "budget": "%d burn-in + %d recorded iterations (9 proposals each)" % (nb, ni),
-                   "fisher": "half the burn-in with one-parameter proposals, then block "
-                             "proposals along the Fisher information of each sequence's best "
-                             "replica (adjoint-gradient Hessian)"},
+                   "fisher": "a quarter of the burn-in with one-parameter proposals; L-BFGS "
+                             "polish of the best replica on the CUDA adjoint; Fisher information "
+                             "there (adjoint-gradient Hessian); restart of all replicas around "
+                             "it; block proposals for the rest"},
         "plain": {"value": float(ess_p.min() / tp), "s": tp, "ess": ess_p.tolist()},
         "fisher": {"value": float(ess_f.min() / tf), "s": tf, "ess": ess_f.tolist()},
         "speedup": float((ess_f.min() / tf) / (ess_p.min() / tp)),
@@ -526,6 +527,97 @@ def run_ess(args, rank, world, local):
     print(json.dumps(line))
 
 
+def run_ess_batch(args, rank, world, local):
+    """ESS per second over many independent fits: the plain per-fit form (one
+    cmc_run per fit, the reference's proposals) against the fused form (all
+    fits in persistent work-list launches; after a quarter of the burn-in,
+    polish + Fisher information + restart + block proposals), same fits,
+    replicas and iteration budget."""
+    import torch
+    from cuda_mcmc_gb300 import fit, synth
+    from cuda_mcmc_gb300.device import BatchJob, DeviceJob
+    from cuda_mcmc_gb300.grad import SgraChi2
+    nb, ni = args.ess_burn, args.ess_iter
+    fits = synth.sgra_batch(nfits=args.nfits, seed=5 + rank, nseq=16, nbeta=16,
+                            nvis_min=500, nvis_max=20000)
+    objs = [SgraChi2.from_workload(w) for w in fits]
+
+    def jobs_for(seed):
+        return [DeviceJob.from_workload(w, niter_total=ni, seed=seed + i) for i, w in enumerate(fits)]
+
+    def plain(jobs):
+        for j in jobs:
+            j.run(nb, 0, do_init=True)
+        for j in jobs:
+            j.run(0, ni, itr0=0)
+
+    def fused(jobs):
+        n1 = nb // 4
+        b = BatchJob(jobs)
+        b.run(n1, 0, do_init=True)
+        torch.cuda.synchronize()
+        for j, o in zip(jobs, objs):
+            fit.fisher_setup(j, o)
+        b = BatchJob(jobs)            # descriptors now carry the block proposals
+        b.run(nb - n1, 0)
+        b.run(0, ni, itr0=0)
+
+    def timed(fn, jobs):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn(jobs)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        for j in jobs:
+            j.check()
+        return dt, [fit.posterior_summary(j.t["pout"].cpu().numpy()) for j in jobs]
+
+    saved = (nb, ni)
+    nb, ni = 10, 10                   # warm-up: library loads, allocator
+    timed(plain, jobs_for(1))
+    timed(fused, jobs_for(1))
+    nb, ni = saved
+    with Clocks(local) as clk:
+        tp, ep = timed(plain, jobs_for(100))
+        tf, ef = timed(fused, jobs_for(100))
+    # reference posteriors: the fused schedule with 4x the recorded iterations
+    ni = 4 * ni
+    _, el = timed(fused, jobs_for(500))
+    ni = saved[1]
+    if rank != 0:
+        return
+
+    def zmax(x, y):
+        return [float(np.max(np.abs(a["mean"] - b["mean"]) / np.sqrt(a["mcse"] ** 2 + b["mcse"] ** 2)))
+                for a, b in zip(x, y)]
+
+    def sdr(x, y):
+        return [float(np.max(np.abs(np.log(a["sd"] / b["sd"])))) for a, b in zip(x, y)]
+
+    acc = {"z_mean_max_plain_vs_long": zmax(ep, el), "z_mean_max_fused_vs_long": zmax(ef, el),
+           "abs_log_sd_ratio_max_plain_vs_long": sdr(ep, el),
+           "abs_log_sd_ratio_max_fused_vs_long": sdr(ef, el),
+           "long_run": "fused schedule, %d recorded iterations, other seeds" % (4 * ni)}
+    ep = [float(x["ess"].min()) for x in ep]
+    ef = [float(x["ess"].min()) for x in ef]
+    vp, vf = float(np.sum(ep) / tp), float(np.sum(ef) / tf)
+    line = {
+        "metric": "ESS/sec over fits (sum over fits of min-over-parameter ESS, T=1 slot)",
+        "value": vf, "unit": "ESS/s", "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": 1e3 * tf, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "%d independent sgra9 fits, nvis logU(500,20000), ncph 0.3 nvis, "
+                               "16x16 replicas each" % len(fits),
+                   "budget": "%d burn-in + %d recorded iterations" % (nb, ni)},
+        "plain_per_fit": {"value": vp, "s": tp, "min_ess_per_fit": [float(x) for x in ep]},
+        "fused": {"value": vf, "s": tf, "min_ess_per_fit": [float(x) for x in ef]},
+        "speedup": vf / vp,
+        "accuracy": acc,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args)
@@ -533,6 +625,8 @@ def main():
         run_batch(args, rank, world, local)
     elif args.impl == "mine" and args.workload == "ess":
         run_ess(args, rank, world, local)
+    elif args.impl == "mine" and args.workload == "ess-batch":
+        run_ess_batch(args, rank, world, local)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

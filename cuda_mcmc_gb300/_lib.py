@@ -120,6 +120,10 @@ def _declare(L):
         L.cmc_grad_work_bytes.restype = C.c_size_t
         L.cmc_grad.argtypes = [C.POINTER(CmcJob), C.c_void_p, C.c_void_p]
         L.cmc_grad.restype = C.c_int
+        L.cmc_fisher_work_bytes.argtypes = [C.POINTER(CmcJob)]
+        L.cmc_fisher_work_bytes.restype = C.c_size_t
+        L.cmc_fisher.argtypes = [C.POINTER(CmcJob), C.c_void_p, C.c_void_p]
+        L.cmc_fisher.restype = C.c_int
     if L.cmc_sizeof_job() != C.sizeof(CmcJob):
         raise RuntimeError("cmc_job layout mismatch between %s and _lib.CmcJob" % L._name)
 

@@ -135,3 +135,41 @@ extern "C" int cmc_grad(const cmc_job *job, float *grad, void *stream)
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CMC_OK : cmc::cuda_fail(e, "sgra_grad_kernel launch");
 }
+
+// cmc_fisher: Gauss-Newton Fisher information of chi^2/2 at pcur for every
+// replica into fisher[ist][nptot][nptot] (zeros for flag[ist] == 0 with flag
+// non-NULL).  job->work: the packed data followed by per-point derivative rows
+// of every replica, cmc_fisher_work_bytes(job) bytes.
+extern "C" size_t cmc_fisher_work_bytes(const cmc_job *job)
+{
+  if (!job) return 0;
+  cmc::SgraModel::Packed pk;
+  const char *err = nullptr;
+  cmc_job k = *job;
+  k.datm = nullptr;
+  if (cmc::SgraModel::host_dims(k, 0, pk, &err)) return 0;
+  const size_t nrep = (size_t)job->nbeta * job->nseq;
+  return grad_extra_offset(pk) + nrep * cmc::sgra_fisher_gwork_floats(pk) * sizeof(float);
+}
+
+extern "C" int cmc_fisher(const cmc_job *job, float *fisher, void *stream)
+{
+  cmc::last_error().clear();
+  if (!job) return cmc::fail(CMC_ERR_ARG, "cmc_fisher: job is NULL");
+  if (!fisher) return cmc::fail(CMC_ERR_ARG, "cmc_fisher: fisher must be a device pointer");
+  const cmc_job &j = *job;
+  cmc::SgraModel::Packed pk;
+  int rc = grad_dims(j, pk);
+  if (rc) return rc;
+  const size_t need = cmc_fisher_work_bytes(job);
+  if (j.work == nullptr || j.work_bytes < need)
+    return cmc::fail(CMC_ERR_ARG, "cmc_fisher: job.work is smaller than cmc_fisher_work_bytes()");
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = cmc::SgraModel::host_pack(j, pk, j.work, s);
+  if (rc) return cmc::fail(rc, "packing the model data failed");
+  float *gwork = (float *)((unsigned char *)j.work + grad_extra_offset(pk));
+  const unsigned nrep = (unsigned)(j.nbeta * j.nseq);
+  cmc::sgra_fisher_kernel<<<nrep, 256, cmc::sgra_fisher_smem(j.nptot), s>>>(j, pk, fisher, gwork);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CMC_OK : cmc::cuda_fail(e, "sgra_fisher_kernel launch");
+}

@@ -245,40 +245,38 @@ __device__ __forceinline__ void sgra_vis_bwd(const float (&C)[kNC], int ring, co
   cb[kSth] += U_bar * v;
 }
 
-// One CTA per replica (ist = blockIdx.x): chi^2 and dchi^2/dp.  Shared
-// memory: the Bessel tables, C, dC/dp [kNC][nptot] and the reductions;
-// per-point phases and adjoints live in gwork[ist][3][npts] (global).
-__global__ void __launch_bounds__(256) sgra_grad_kernel(const cmc_job job,
-                                                        const SgraModel::Packed pk, float *grad,
-                                                        float *gwork)
+// Per-CTA prologue of the gradient and Fisher kernels for replica ist: the
+// Bessel tables into shared memory, the constants C and their Jacobian
+// dC/dp [kNC][nptot] (forward mode, thread k < nptot differentiates along
+// parameter k).  Layout of the dynamic shared memory: btab | tab3 | C [kNC] |
+// jac [kNC][nptot] | p [kMaxGradParams] | flags [3] | rest (returned).
+struct GradCta {
+  const float4 *btab;
+  const float *tab3;
+  const float *jac;
+  float C[kNC];
+  SgraConsts sc;
+  int ring;
+  float *rest;
+};
+
+__device__ inline GradCta grad_prologue(const cmc_job &job, const SgraModel::Packed &pk, int ist,
+                                        unsigned char *smem)
 {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5, lane = tid & 31, warp = tid >> 5;
-  const int ist = blockIdx.x, nptot = job.nptot, npts = pk.npts;
-  const bool active = job.flag == nullptr || job.flag[ist] != 0;
-  if (!active) {   // uniform over the CTA
-    for (int k = tid; k < nptot; k += T) grad[(size_t)ist * nptot + k] = 0.0f;
-    if (tid == 0) job.chi2c[ist] = 0.0f;
-    return;
-  }
+  const int tid = threadIdx.x, T = blockDim.x, nptot = job.nptot;
   float4 *btab = reinterpret_cast<float4 *>(smem);
   const int ntab = kBesselIntervals * ((kBesselDeg + 1) / 2);
   float *tab3 = reinterpret_cast<float *>(btab + ntab);
-  float *Cs = tab3 + kBesselIntervals * (kBesselDeg + 1);   // [kNC]
-  float *jac = Cs + kNC;                                      // [kNC][nptot]
-  float *red = jac + kNC * nptot;                             // [kNC + 1][NW]
-  float *ph = gwork + (size_t)ist * 3 * npts;                 // [npts] phases
-  float *abar = ph + npts;                                    // [npts] d chi2 / d|V|
-  float *pbar = abar + npts;                                  // [npts] d chi2 / d phase
-  __shared__ int s_flags[3];
-  __shared__ float s_p[kMaxGradParams];
+  float *Cs = tab3 + kBesselIntervals * (kBesselDeg + 1);
+  float *jac = Cs + kNC;
+  float *s_p = jac + kNC * nptot;
+  int *s_flags = reinterpret_cast<int *>(s_p + kMaxGradParams);
   for (int i = tid; i < ntab; i += T) btab[i] = (&kBesselTab[0][0])[i];
   for (int i = tid; i < kBesselIntervals * (kBesselDeg + 1); i += T)
     tab3[i] = (&kBesselTab3[0][0])[i];
   for (int i = tid; i < nptot; i += T) s_p[i] = job.pcur[(size_t)ist * nptot + i];
   __syncthreads();
   if (tid < nptot) {
-    // column tid of dC/dp: forward mode along parameter tid
     Dual pd[kMaxGradParams];
 #pragma unroll
     for (int j = 0; j < kMaxGradParams; ++j)
@@ -295,23 +293,58 @@ __global__ void __launch_bounds__(256) sgra_grad_kernel(const cmc_job job,
     }
   }
   __syncthreads();
-  float C[kNC];
+  GradCta g;
+  g.btab = btab;
+  g.tab3 = tab3;
+  g.jac = jac;
 #pragma unroll
-  for (int j = 0; j < kNC; ++j) C[j] = Cs[j];
-  const int ring = s_flags[2];
-  SgraConsts sc;
-  sc.cth = C[kCth]; sc.sth = C[kSth]; sc.kex = C[kKex]; sc.kin = C[kKin];
-  sc.ae = C[kAe]; sc.be = C[kBe]; sc.ai = C[kAi]; sc.bi = C[kBi]; sc.dsh = C[kDsh];
-  sc.gc = C[kGc]; sc.gs = C[kGs]; sc.gx = C[kGx]; sc.gy = C[kGy]; sc.gpu = C[kGpu];
-  sc.gpv = C[kGpv]; sc.zr = C[kZr]; sc.zg = C[kZg];
-  sc.inner = s_flags[0]; sc.gauss = s_flags[1]; sc.ring = ring; sc.bigx = 1;
+  for (int j = 0; j < kNC; ++j) g.C[j] = Cs[j];
+  g.ring = s_flags[2];
+  SgraConsts &sc = g.sc;
+  sc.cth = g.C[kCth]; sc.sth = g.C[kSth]; sc.kex = g.C[kKex]; sc.kin = g.C[kKin];
+  sc.ae = g.C[kAe]; sc.be = g.C[kBe]; sc.ai = g.C[kAi]; sc.bi = g.C[kBi]; sc.dsh = g.C[kDsh];
+  sc.gc = g.C[kGc]; sc.gs = g.C[kGs]; sc.gx = g.C[kGx]; sc.gy = g.C[kGy]; sc.gpu = g.C[kGpu];
+  sc.gpv = g.C[kGpv]; sc.zr = g.C[kZr]; sc.zg = g.C[kZg];
+  sc.inner = s_flags[0]; sc.gauss = s_flags[1]; sc.ring = g.ring; sc.bigx = 1;
+  g.rest = reinterpret_cast<float *>(s_flags + 4);
+  return g;
+}
+
+inline size_t grad_prologue_floats(int nptot)
+{
+  return (size_t)kBesselIntervals * ((kBesselDeg + 1) / 2) * 4 +
+         (size_t)kBesselIntervals * (kBesselDeg + 1) + kNC + (size_t)kNC * nptot +
+         kMaxGradParams + 4;
+}
+
+// One CTA per replica (ist = blockIdx.x): chi^2 and dchi^2/dp.  Shared
+// memory: the prologue, then the reductions [kNC + 1][NW]; per-point phases
+// and adjoints live in gwork[ist][3][npts] (global).
+__global__ void __launch_bounds__(256) sgra_grad_kernel(const cmc_job job,
+                                                        const SgraModel::Packed pk, float *grad,
+                                                        float *gwork)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5, lane = tid & 31, warp = tid >> 5;
+  const int ist = blockIdx.x, nptot = job.nptot, npts = pk.npts;
+  const bool active = job.flag == nullptr || job.flag[ist] != 0;
+  if (!active) {   // uniform over the CTA
+    for (int k = tid; k < nptot; k += T) grad[(size_t)ist * nptot + k] = 0.0f;
+    if (tid == 0) job.chi2c[ist] = 0.0f;
+    return;
+  }
+  const GradCta g = grad_prologue(job, pk, ist, smem);
+  float *red = g.rest;                                        // [kNC + 1][NW]
+  float *ph = gwork + (size_t)ist * 3 * npts;                 // [npts] phases
+  float *abar = ph + npts;                                    // [npts] d chi2 / d|V|
+  float *pbar = abar + npts;                                  // [npts] d chi2 / d phase
   float c2 = 0.0f;
   // pass A: amplitude terms, amplitude adjoints, phases
   for (int i = tid; i < npts; i += T) {
     const float4 d = __ldg(&pk.vis[i]);
     const float rho = __ldg(&pk.rho[i]);
     float2 V;
-    sgra_vis_acc(sc, ring, btab, d.x, d.y, rho, V);
+    sgra_vis_acc(g.sc, g.ring, g.btab, d.x, d.y, rho, V);
     const float A = sqrtf(fmaf(V.x, V.x, V.y * V.y));
     const float r = d.z - A;
     c2 = fmaf(r * r, d.w, c2);
@@ -326,12 +359,12 @@ __global__ void __launch_bounds__(256) sgra_grad_kernel(const cmc_job job,
       const int4 q = __ldg(&pk.cli[c]);
       const float4 f = __ldg(&pk.clf[c]);
       const float x = f.w - (ph[q.x] + ph[q.y] - ph[q.z]);
-      const float dw = x - 6.2831853071795865f * rintf(x * 0.15915494309189535f);
+      const float dw = fmaf(-6.2831853071795865f, rintf(x * 0.15915494309189535f), x);
       c2 = fmaf(dw * dw, f.z, c2);
-      const float g = -2.0f * f.z * dw;
-      atomicAdd(&pbar[q.x], g);
-      atomicAdd(&pbar[q.y], g);
-      atomicAdd(&pbar[q.z], -g);
+      const float gg = -2.0f * f.z * dw;
+      atomicAdd(&pbar[q.x], gg);
+      atomicAdd(&pbar[q.y], gg);
+      atomicAdd(&pbar[q.z], -gg);
     }
   }
   __syncthreads();
@@ -345,48 +378,148 @@ __global__ void __launch_bounds__(256) sgra_grad_kernel(const cmc_job job,
     const float ab = abar[i], pb = pbar[i];
     if (ab == 0.0f && pb == 0.0f) continue;
     float2 V;
-    sgra_vis_acc(sc, ring, btab, d.x, d.y, rho, V);
+    sgra_vis_acc(g.sc, g.ring, g.btab, d.x, d.y, rho, V);
     const float n2 = fmaf(V.x, V.x, V.y * V.y);
     if (!(n2 > 0.0f)) continue;
     const float A = sqrtf(n2);
     const float vre_bar = ab * V.x / A - pb * V.y / n2;
     const float vim_bar = ab * V.y / A + pb * V.x / n2;
-    sgra_vis_bwd(C, ring, btab, tab3, d.x, d.y, rho, vre_bar, vim_bar, cb);
+    sgra_vis_bwd(g.C, g.ring, g.btab, g.tab3, d.x, d.y, rho, vre_bar, vim_bar, cb);
   }
   // reduce cb[kNC] and c2 over the CTA
 #pragma unroll
   for (int j = 0; j < kNC; ++j) {
-    const float s = warp_sum(cb[j]);
-    if (lane == 0) red[j * NW + warp] = s;
+    const float sum = warp_sum(cb[j]);
+    if (lane == 0) red[j * NW + warp] = sum;
   }
   {
-    const float s = warp_sum(c2);
-    if (lane == 0) red[kNC * NW + warp] = s;
+    const float sum = warp_sum(c2);
+    if (lane == 0) red[kNC * NW + warp] = sum;
   }
   __syncthreads();
   if (tid < nptot) {
-    float g = 0.0f;
+    float gk = 0.0f;
     for (int j = 0; j < kNC; ++j) {
       float cbj = 0.0f;
       for (int w = 0; w < NW; ++w) cbj += red[j * NW + w];
-      g = fmaf(cbj, jac[j * nptot + tid], g);
+      gk = fmaf(cbj, g.jac[j * nptot + tid], gk);
     }
-    grad[(size_t)ist * nptot + tid] = g;
+    grad[(size_t)ist * nptot + tid] = gk;
   }
   if (tid == 0) {
-    float s = 0.0f;
-    for (int w = 0; w < NW; ++w) s += red[kNC * NW + w];
-    job.chi2c[ist] = s;
+    float sum = 0.0f;
+    for (int w = 0; w < NW; ++w) sum += red[kNC * NW + w];
+    job.chi2c[ist] = sum;
   }
+}
+
+// Gauss-Newton Fisher information of chi^2/2 for replica ist = blockIdx.x:
+//   F = sum_i w_i dA_i dA_i^T + sum_c w_c dphi_c dphi_c^T,
+// dA_i, dphi_c the gradients with respect to p of the model amplitude of
+// visibility i and of the closure phase c (dphi_c = dphi_i + dphi_j - dphi_k).
+// Per point, dV/dC comes from two reverse sweeps (seeds 1 and i); then
+// F_C [kNC][kNC] accumulates in C-space and F = dC/dp^T F_C dC/dp.
+// gwork[ist]: amplitude rows [npts][kNC + 1] (dA/dC, w), phase rows
+// [npts][kNC] (dphi/dC), closure rows [ncph][kNC + 1].
+__global__ void __launch_bounds__(256) sgra_fisher_kernel(const cmc_job job,
+                                                          const SgraModel::Packed pk,
+                                                          float *fisher, float *gwork)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int ist = blockIdx.x, nptot = job.nptot, npts = pk.npts;
+  const int ncph = (pk.npass >= 2) ? pk.ncph : 0;
+  constexpr int W1 = kNC + 1;
+  const bool active = job.flag == nullptr || job.flag[ist] != 0;
+  if (!active) {
+    for (int k = tid; k < nptot * nptot; k += T) fisher[(size_t)ist * nptot * nptot + k] = 0.0f;
+    return;
+  }
+  const GradCta g = grad_prologue(job, pk, ist, smem);
+  float *FC = g.rest;                                          // [kNC][kNC]
+  float *arow = gwork + (size_t)ist * ((size_t)npts * (W1 + kNC) + (size_t)ncph * W1);
+  float *prow = arow + (size_t)npts * W1;
+  float *crow = prow + (size_t)npts * kNC;
+  for (int i = tid; i < npts; i += T) {
+    const float4 d = __ldg(&pk.vis[i]);
+    const float rho = __ldg(&pk.rho[i]);
+    float2 V;
+    sgra_vis_acc(g.sc, g.ring, g.btab, d.x, d.y, rho, V);
+    const float n2 = fmaf(V.x, V.x, V.y * V.y);
+    float cr[kNC], ci[kNC];
+#pragma unroll
+    for (int j = 0; j < kNC; ++j) cr[j] = ci[j] = 0.0f;
+    const bool ok = n2 > 0.0f;
+    if (ok) {
+      sgra_vis_bwd(g.C, g.ring, g.btab, g.tab3, d.x, d.y, rho, 1.0f, 0.0f, cr);
+      sgra_vis_bwd(g.C, g.ring, g.btab, g.tab3, d.x, d.y, rho, 0.0f, 1.0f, ci);
+    }
+    const float ia = ok ? rsqrtf(n2) : 0.0f, in2 = ok ? 1.0f / n2 : 0.0f;
+#pragma unroll
+    for (int j = 0; j < kNC; ++j) {
+      arow[(size_t)i * W1 + j] = (V.x * cr[j] + V.y * ci[j]) * ia;
+      prow[(size_t)i * kNC + j] = (V.x * ci[j] - V.y * cr[j]) * in2;
+    }
+    arow[(size_t)i * W1 + kNC] = d.w;
+  }
+  __syncthreads();
+  for (int c = tid; c < ncph; c += T) {
+    const int4 q = __ldg(&pk.cli[c]);
+    const float4 f = __ldg(&pk.clf[c]);
+#pragma unroll
+    for (int j = 0; j < kNC; ++j)
+      crow[(size_t)c * W1 + j] = prow[(size_t)q.x * kNC + j] + prow[(size_t)q.y * kNC + j] -
+                                 prow[(size_t)q.z * kNC + j];
+    crow[(size_t)c * W1 + kNC] = f.z;
+  }
+  __syncthreads();
+  // F_C: one thread per upper-triangle entry (j <= l)
+  constexpr int kPairs = kNC * (kNC + 1) / 2;
+  for (int e = tid; e < kPairs; e += T) {
+    int j = 0, rem = e;
+    while (rem >= kNC - j) { rem -= kNC - j; ++j; }
+    const int l = j + rem;
+    float acc = 0.0f;
+    for (int i = 0; i < npts; ++i) {
+      const float *r = arow + (size_t)i * W1;
+      acc = fmaf(r[kNC] * r[j], r[l], acc);
+    }
+    for (int c = 0; c < ncph; ++c) {
+      const float *r = crow + (size_t)c * W1;
+      acc = fmaf(r[kNC] * r[j], r[l], acc);
+    }
+    FC[j * kNC + l] = acc;
+    FC[l * kNC + j] = acc;
+  }
+  __syncthreads();
+  for (int e = tid; e < nptot * nptot; e += T) {
+    const int a = e / nptot, b = e - a * nptot;
+    float acc = 0.0f;
+    for (int j = 0; j < kNC; ++j) {
+      const float ja = g.jac[j * nptot + a];
+      if (ja == 0.0f) continue;
+      float t = 0.0f;
+      for (int l = 0; l < kNC; ++l) t = fmaf(FC[j * kNC + l], g.jac[l * nptot + b], t);
+      acc = fmaf(ja, t, acc);
+    }
+    fisher[(size_t)ist * nptot * nptot + e] = acc;
+  }
+}
+
+inline size_t sgra_fisher_gwork_floats(const SgraModel::Packed &pk)
+{
+  const size_t ncph = (pk.npass >= 2) ? (size_t)pk.ncph : 0;
+  return (size_t)pk.npts * (2 * kNC + 1) + ncph * (kNC + 1);
+}
+
+inline size_t sgra_fisher_smem(int nptot)
+{
+  return (grad_prologue_floats(nptot) + (size_t)kNC * kNC) * 4;
 }
 
 inline size_t sgra_grad_smem(int nptot, int T)
 {
-  const int NW = T / 32;
-  const size_t floats = (size_t)kBesselIntervals * ((kBesselDeg + 1) / 2) * 4 +
-                        (size_t)kBesselIntervals * (kBesselDeg + 1) + kNC +
-                        (size_t)kNC * nptot + (size_t)(kNC + 1) * NW;
-  return floats * 4;
+  return (grad_prologue_floats(nptot) + (size_t)(kNC + 1) * (T / 32)) * 4;
 }
 
 }  // namespace cmc

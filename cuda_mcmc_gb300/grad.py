@@ -4,6 +4,9 @@
   through the hand-written CUDA adjoint (``cmc_grad`` in libcmc_sgra.so);
   :meth:`SgraChi2.chi2` is differentiable (a ``torch.autograd.Function`` whose
   backward is that adjoint).
+* :meth:`SgraChi2.fisher_gn` -- the Gauss-Newton Fisher information of
+  chi^2/2 (``cmc_fisher``: per-datum model gradients from the adjoint,
+  accumulated on the GPU); always positive semi-definite;
 * :func:`fisher` -- the observed Fisher information of the tempered posterior
   exp(-beta chi^2 / 2): beta/2 times the Hessian of chi^2, from central
   differences of the adjoint gradient (one batched call for all 2 k
@@ -94,6 +97,33 @@ class SgraChi2:
     def chi2(self, p):
         """Differentiable chi^2 [n] of p[n, nptot]: backward is the CUDA adjoint."""
         return _Chi2Fn.apply(p, self)
+
+    def fisher_gn(self, p, stream=None):
+        """Gauss-Newton Fisher information of chi^2/2, [n, nptot, nptot], at
+        p[n, nptot] (cmc_fisher): sum over data of w * grad(model) grad(model)^T
+        for the amplitudes and the closure phases."""
+        p = torch.as_tensor(p, dtype=_F32).to(self.device).contiguous()
+        if p.dim() != 2 or p.shape[1] != self.nptot:
+            raise ValueError("p must be [n, %d]" % self.nptot)
+        n = int(p.shape[0])
+        out = torch.empty((n, self.nptot, self.nptot), dtype=_F32, device=self.device)
+        chi2 = torch.empty(max(n, 1), dtype=_F32, device=self.device)
+        if n == 0:
+            return out
+        j = self.job
+        j.nbeta = n
+        j.ndatm = 0
+        j.pcur, j.chi2c, j.flag = p.data_ptr(), chi2.data_ptr(), None
+        need = int(self.L.cmc_fisher_work_bytes(C.byref(j)))
+        if need == 0:
+            raise _lib.McmcError(_lib.CMC_ERR_ARG, "cmc_fisher_work_bytes: invalid job")
+        if self._work is None or self._work.numel() < need:
+            self._work = torch.empty(need, dtype=torch.uint8, device=self.device)
+        j.work, j.work_bytes = self._work.data_ptr(), int(self._work.numel())
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(self.L, self.L.cmc_fisher(C.byref(j), C.c_void_p(out.data_ptr()),
+                                             C.c_void_p(s.cuda_stream)))
+        return out
 
 
 class _Chi2Fn(torch.autograd.Function):

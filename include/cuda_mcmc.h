@@ -125,6 +125,17 @@ int cmc_eval(const cmc_job *job, int mode, void *stream);
 size_t cmc_grad_work_bytes(const cmc_job *job);
 int cmc_grad(const cmc_job *job, float *grad, void *stream);
 
+/* Gauss-Newton Fisher information of chi^2/2 (libcmc_sgra.so only; no
+ * counterpart in the reference):
+ *   fisher[ist][a][b] = sum_i w_i dA_i/dp_a dA_i/dp_b
+ *                     + sum_c w_c dphi_c/dp_a dphi_c/dp_b
+ * over the amplitude terms i and (npass >= 2) the closure-phase terms c of
+ * the chi^2 above, at p = pcur[ist] for every replica (zeros where flag[ist]
+ * == 0).  Same inputs as cmc_grad; job->work of at least
+ * cmc_fisher_work_bytes(job) bytes.  Asynchronous on `stream`. */
+size_t cmc_fisher_work_bytes(const cmc_job *job);
+int cmc_fisher(const cmc_job *job, float *fisher, void *stream);
+
 /* ---- batches of independent jobs (fits) ------------------------------------
  * No counterpart in the reference (it runs one fit per mcmc_cuda call).
  * Every job is a complete cmc_job (device arrays, own sizes; all with the same

@@ -152,3 +152,32 @@ def chi2_and_grad(prm, coor, dat, std2r, icoor, nvis, npass=2, imodel=1):
     c = chi2(p, coor, dat, std2r, icoor, nvis, npass, imodel)
     (g,) = torch.autograd.grad(c.sum(), p)
     return c.detach().numpy(), g.numpy()
+
+
+def residuals(prm, coor, dat, std2r, icoor, nvis, npass=2, imodel=1):
+    """Weighted residuals r with chi^2 = sum r^2 for one parameter row prm
+    [nptot]: sqrt(w) (amp_obs - |V|) for the amplitudes, then
+    sqrt(w) wrap(cph_obs - cph) for the closure phases (npass >= 2)."""
+    t = lambda a, dt=torch.float64: torch.as_tensor(np.asarray(a), dtype=dt)
+    coor = t(coor)
+    u, v = coor[0:2 * nvis:2], coor[1:2 * nvis:2]
+    dat, std2r = t(dat), t(std2r)
+    re, im = vis(prm[None, :], u, v, imodel)
+    amp = torch.sqrt(re * re + im * im)[0]
+    r = torch.sqrt(std2r[:nvis]) * (dat[:nvis] - amp)
+    ncph = dat.numel() - nvis
+    if npass >= 2 and ncph > 0:
+        ph = torch.atan2(im, re)[0]
+        tri = t(icoor, torch.int64)[:3 * ncph].reshape(ncph, 3)
+        x = dat[nvis:] - (ph[tri[:, 0]] + ph[tri[:, 1]] - ph[tri[:, 2]])
+        r = torch.cat([r, torch.sqrt(std2r[nvis:]) * torch.atan2(torch.sin(x), torch.cos(x))])
+    return r
+
+
+def fisher_gn(prm, coor, dat, std2r, icoor, nvis, npass=2, imodel=1):
+    """Gauss-Newton Fisher information J^T J of chi^2/2 (J = d residuals / d prm)
+    at one parameter row, float64 [nptot, nptot]."""
+    p = torch.as_tensor(np.asarray(prm, np.float64))
+    J = torch.autograd.functional.jacobian(
+        lambda x: residuals(x, coor, dat, std2r, icoor, nvis, npass, imodel), p)
+    return (J.T @ J).numpy()

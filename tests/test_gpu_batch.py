@@ -34,7 +34,7 @@ def test_batch_equals_individual_runs_with_the_class_shape():
     batch.run(nburn, 0, do_init=True)
     batch.run(0, niter)
     batch.check()
-    # which class (shape) each fit landed in: classes are filled in size order
+    # the batch does not report which class a fit landed in: try each shape
     for i, w in enumerate(fits):
         got = jobs[i].to_numpy()
         ref = DeviceJob.from_workload(w, niter_total=niter, seed=100 + i)
@@ -49,9 +49,12 @@ def test_batch_equals_individual_runs_with_the_class_shape():
             except _lib.McmcError:
                 continue
             r = ref2.to_numpy()
-            if np.array_equal(r["pout"], got["pout"]) and np.array_equal(r["rndst"], got["rndst"]):
-                for f in ("chi2", "tout", "pcur", "chi2c", "n_acpt", "n_exch", "n_hist", "pstp"):
-                    assert np.array_equal(r[f], got[f]), f
+            # every shape makes the same decisions here (so pout and the
+            # generator states agree for all of them); the chi^2 sums of the
+            # fit's own class shape match to the bit
+            fields = ("pout", "rndst", "chi2", "tout", "pcur", "chi2c", "n_acpt", "n_exch",
+                      "n_hist", "pstp")
+            if all(np.array_equal(r[f], got[f]) for f in fields):
                 matched = True
                 break
         assert matched, "fit %d: the batch result matches no single-job run" % i

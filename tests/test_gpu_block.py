@@ -99,14 +99,12 @@ def test_block_batch_equals_single_launches():
     fits = [synth.sgra(nvis=nv, ncph=nc, seed=60 + i, nseq=2, nbeta=8)
             for i, (nv, nc) in enumerate([(150, 45), (900, 270)])]
     nburn, niter = 5, 6
-    jobs, refs = [], []
+    jobs = []
     for i, w in enumerate(fits):
-        L = _chol(w, w.nseq, seed=10 + i)
-        for lst in (jobs, refs):
-            j = DeviceJob.from_workload(w, niter_total=niter, seed=300 + i)
-            j.run(0, 0, do_init=True)
-            j.set_block_proposals(L)
-            lst.append(j)
+        j = DeviceJob.from_workload(w, niter_total=niter, seed=300 + i)
+        j.run(0, 0, do_init=True)
+        j.set_block_proposals(_chol(w, w.nseq, seed=10 + i))
+        jobs.append(j)
     batch = BatchJob(jobs)
     classes = batch.classes()
     batch.run(nburn, 0)
@@ -127,9 +125,10 @@ def test_block_batch_equals_single_launches():
             except _lib.McmcError:
                 continue
             r = ref.to_numpy()
-            if np.array_equal(r["rndst"], got["rndst"]) and np.array_equal(r["pout"], got["pout"]):
-                for f in ("chi2", "tout", "pcur", "chi2c", "n_acpt", "pstp"):
-                    assert np.array_equal(r[f], got[f]), f
+            # all shapes may make the same decisions; the fit's own class shape
+            # also sums chi^2 in the same order, to the bit
+            if all(np.array_equal(r[f], got[f]) for f in ("rndst", "pout", "chi2", "tout",
+                                                           "pcur", "chi2c", "n_acpt", "pstp")):
                 ok = True
                 break
         assert ok, "fit %d matched no class shape" % i

@@ -221,6 +221,37 @@ def test_autograd_function_and_flags(big):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("imodel", [1, 2])
+def test_gauss_newton_fisher_matches_autograd_jacobian(imodel):
+    """cmc_fisher against J^T J from torch.autograd's Jacobian of the weighted
+    residuals of the FP64 re-expression, at 3 seeded points: relative
+    Frobenius error 1e-4."""
+    from cuda_mcmc_gb300.grad import SgraChi2
+    w = synth.sgra(nvis=2000, ncph=600, seed=3, nseq=2, nbeta=4)
+    nptot = 9 if imodel == 1 else 13
+    obj = SgraChi2(w.coor, w.dat, w.std2r, w.icoor, w.idat, nptot, imodel, w.npass)
+    P = _points(w, 3, imodel, seed=13)
+    F = obj.fisher_gn(P.astype(np.float32)).double().cpu().numpy()
+    for q in range(P.shape[0]):
+        want = torch_sgra.fisher_gn(P[q], w.coor, w.dat, w.std2r, w.icoor, int(w.idat[0]),
+                                    w.npass, imodel)
+        rel = np.linalg.norm(F[q] - want) / np.linalg.norm(want)
+        assert rel < 1e-4, (q, rel)
+
+
+def test_torch_gauss_newton_fisher_is_jtj_of_the_chi2():
+    """CPU pin of the test-side Gauss-Newton reference: sum r^2 is the chi^2."""
+    w = synth.sgra(nvis=200, ncph=60, nseq=2, nbeta=4)
+    P = _points(w, 2, 1, seed=4)
+    for p in P:
+        r = torch_sgra.residuals(torch.tensor(p), w.coor, w.dat, w.std2r, w.icoor,
+                                 int(w.idat[0]), w.npass, 1)
+        c = torch_sgra.chi2(torch.tensor(p)[None], w.coor, w.dat, w.std2r, w.icoor,
+                            int(w.idat[0]), w.npass, 1)
+        np.testing.assert_allclose(float((r * r).sum()), float(c[0]), rtol=1e-12)
+
+
+@pytest.mark.gpu
 def test_fisher_matches_the_autograd_hessian():
     from cuda_mcmc_gb300 import grad
     w = synth.sgra(nvis=2000, ncph=600, seed=3, nseq=2, nbeta=4)
@@ -264,3 +295,20 @@ def test_polish_descends_to_the_fit():
     ref = minimize(f64, p, jac=True, method="L-BFGS-B", bounds=list(zip(lo, hi)),
                    options={"maxiter": 500, "ftol": 1e-15, "gtol": 1e-10})
     assert c_at_p - ref.fun <= 1e-5 * ref.fun, (c_at_p, ref.fun)
+
+
+def test_covariance_and_jittered_cholesky_of_ill_conditioned_information():
+    """The Fisher schedule's host algebra: an information matrix with a 1e10
+    eigenvalue spread inverts to a covariance whose Cholesky factor
+    reproduces it; a singular PSD matrix factors with a tiny jitter."""
+    from cuda_mcmc_gb300 import fit
+    rng = np.random.default_rng(5)
+    Q, _ = np.linalg.qr(rng.standard_normal((9, 9)))
+    F = (Q * np.logspace(-2, 8, 9)) @ Q.T
+    C = fit.covariance(F)
+    np.testing.assert_allclose(C @ F, np.eye(9), atol=1e-6)
+    L = fit.cholesky_psd(C)
+    np.testing.assert_allclose(L @ L.T, C, rtol=1e-8, atol=1e-12 * np.abs(C).max())
+    S = np.outer(np.arange(1, 4), np.arange(1, 4)).astype(np.float64)   # rank 1
+    Ls = fit.cholesky_psd(S)
+    np.testing.assert_allclose(Ls @ Ls.T, S, atol=1e-6 * S.max())
