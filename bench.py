@@ -318,7 +318,16 @@ def run_mine(args, rank, world, local):
     from cuda_mcmc_gb300.device import DeviceJob
     _lib.load("sgra")
     w = workload(args, rank)
-    job = DeviceJob.from_workload(w, niter_total=args.main_per_step, seed=1234 + rank)
+    if world > 1:
+        # one run of world*nseq sequences, rank r holding sequences
+        # [r*nseq, (r+1)*nseq): the shards together walk the unsharded chains
+        from cuda_mcmc_gb300 import synth
+        wt = synth.sgra(nvis=args.nvis, ncph=args.ncph, seed=3, nseq=args.nseq * world,
+                        nbeta=args.nbeta, nburn=args.burn_per_step, niter=args.main_per_step)
+        job = DeviceJob.from_workload(wt, niter_total=args.main_per_step, seed=1234,
+                                      seqs=(rank * args.nseq, (rank + 1) * args.nseq))
+    else:
+        job = DeviceJob.from_workload(w, niter_total=args.main_per_step, seed=1234)
     if not args.no_tune:
         job.autotune()
     cfg = job.config()
@@ -365,7 +374,8 @@ def run_mine(args, rank, world, local):
                                                                 w.nbeta),
             "step": "%d burn-in + %d main iterations (9 proposals + exchange each) of all "
                     "replicas = %d chi2 evals" % (args.burn_per_step, args.main_per_step, n_ev),
-            "parallelism": "replicas only (independent sequences per GPU)",
+            "parallelism": "replicas only: sequences sharded across ranks (seq_offset/"
+                           "nseq_total), no collective in the sweep",
             "l2": "2x L2 buffer written between timed steps",
             "launch": cfg},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

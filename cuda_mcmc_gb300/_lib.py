@@ -53,6 +53,7 @@ class CmcJob(C.Structure):
         ("work", _vp), ("work_bytes", C.c_size_t),
         ("status", _vp),
         ("prop_mode", C.c_int), ("prop_reserved", C.c_int), ("prop_chol", _vp),
+        ("seq_offset", C.c_int), ("nseq_total", C.c_int),
     ]
 
 

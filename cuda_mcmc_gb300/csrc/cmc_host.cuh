@@ -192,6 +192,9 @@ inline int validate_common(const cmc_job &j, int mode)
       return fail(CMC_ERR_ARG, "prop_mode must be CMC_PROP_SINGLE (0) or CMC_PROP_BLOCK (1)");
     if (j.prop_mode == CMC_PROP_BLOCK && !j.prop_chol)
       return fail(CMC_ERR_ARG, "block proposals need prop_chol [nseq][nprm][nprm]");
+    if (j.nseq_total < 0 ||
+        (j.nseq_total > 0 && (j.seq_offset < 0 || j.seq_offset + j.nseq > j.nseq_total)))
+      return fail(CMC_ERR_ARG, "sharding: need 0 <= seq_offset and seq_offset + nseq <= nseq_total");
   }
   return CMC_OK;
 }

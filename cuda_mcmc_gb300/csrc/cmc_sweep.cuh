@@ -134,7 +134,12 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
       rng.cu = job.do_init ? 0 : job.inj_cur[2 * ist];
       rng.cn = job.do_init ? 0 : job.inj_cur[2 * ist + 1];
     } else if (job.do_init) {
-      curand_init(job.seed, (unsigned long long)ist, 0ull, &rng.st);
+      // the replica's subsequence in the unsharded run (ist when unsharded)
+      const unsigned long long sub =
+          job.nseq_total > 0
+              ? (unsigned long long)ibeta * job.nseq_total + job.seq_offset + iseq
+              : (unsigned long long)ist;
+      curand_init(job.seed, sub, 0ull, &rng.st);
     } else {
       rng.st = reinterpret_cast<const curandStateXORWOW *>(job.rndst)[ist];
     }

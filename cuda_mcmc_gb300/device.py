@@ -80,7 +80,7 @@ class DeviceJob:
     def __init__(self, model, coor, dat, std2r, icoor, idat, pdescr, pmint, pmaxt, beta,
                  nseq, niter_total, imodel=1, npass=1, nadj=100, ptotal=None, pstp=None,
                  seed=1234, rng="curand", streams=None, ndatm=None, device="cuda",
-                 lib=None):
+                 lib=None, seq_offset=0, nseq_total=0):
         self.L = lib if lib is not None else _lib.load(model)
         self.device = torch.device(device)
         d = self.device
@@ -140,6 +140,13 @@ class DeviceJob:
         j.niter_total = self.niter_total
         j.rng_mode = _lib.CMC_RNG_INJECTED if rng == "injected" else _lib.CMC_RNG_CURAND
         j.seed = int(np.uint64(seed))
+        # a shard of sequences [seq_offset, seq_offset + nseq) of an
+        # nseq_total-sequence run (see cmc_job.h); 0 = unsharded
+        if nseq_total and not (0 <= seq_offset and seq_offset + self.nseq <= nseq_total):
+            raise ValueError("shard [%d, %d) outside 0..%d" % (seq_offset, seq_offset + self.nseq,
+                                                               nseq_total))
+        j.seq_offset, j.nseq_total = int(seq_offset), int(nseq_total)
+        self.seq_offset, self.nseq_total = int(seq_offset), int(nseq_total)
         for i in range(4):
             j.hidat[i] = int(idat[i]) if i < idat.size else 0
         for k in ("coor", "dat", "std2r", "icoor", "idat", "pdescr", "ivar", "invar", "pmint",
@@ -159,11 +166,18 @@ class DeviceJob:
 
     @classmethod
     def from_workload(cls, w, niter_total=None, seed=1234, rng="curand", streams=None,
-                      device="cuda", lib=None):
+                      device="cuda", lib=None, seqs=None):
+        """``seqs`` = (s0, s1): only sequences s0..s1-1 of the workload's nseq
+        (a shard; its chains are those sequences of the unsharded run)."""
+        nseq, off, tot = w.nseq, 0, 0
+        if seqs is not None:
+            off, tot = int(seqs[0]), w.nseq
+            nseq = int(seqs[1]) - off
         return cls(w.model, w.coor, w.dat, w.std2r, w.icoor, w.idat, w.pdescr, w.pmint, w.pmaxt,
-                   w.beta(), w.nseq, w.niter if niter_total is None else niter_total,
+                   w.beta(), nseq, w.niter if niter_total is None else niter_total,
                    imodel=w.imodel, npass=w.npass, ptotal=w.ptotal, pstp=w.pstp0, seed=seed,
-                   rng=rng, streams=streams, device=device, lib=lib)
+                   rng=rng, streams=streams, device=device, lib=lib, seq_offset=off,
+                   nseq_total=tot)
 
     # ---- launching -----------------------------------------------------------
     def run(self, nburn=0, niter=0, do_init=False, itr0=None, stream=None):

@@ -101,6 +101,15 @@ typedef struct cmc_job {
   int prop_mode;
   int prop_reserved;
   const float *prop_chol;
+
+  /* sequence sharding (no counterpart in the reference): when nseq_total > 0
+     this job holds sequences [seq_offset, seq_offset + nseq) of a run with
+     nseq_total sequences, and replica (ibeta, iseq) seeds its generator with
+     curand_init(seed, ibeta*nseq_total + seq_offset + iseq, 0), the
+     subsequence it has in the unsharded run, so that the shards of a run
+     together walk exactly the unsharded run's chains.  0: unsharded. */
+  int seq_offset;
+  int nseq_total;
 } cmc_job;
 
 #ifdef __cplusplus

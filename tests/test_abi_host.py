@@ -48,7 +48,7 @@ def test_library_exports_every_declared_symbol(name):
     missing = want - syms
     assert not missing, "missing exports: %s" % sorted(missing)
     assert L.cmc_sizeof_job() == C.sizeof(_lib.CmcJob)
-    assert L.cmc_abi_version() == 2
+    assert L.cmc_abi_version() == 3
     assert L.cmc_model_name().decode() == name
 
 
