@@ -69,7 +69,7 @@ def candidates(job):
             for T in T_VALUES:
                 if T < 32 * ((R + 31) // 32):
                     continue
-                for ph in (1, 0):
+                for ph in (1, 0, 2):        # 2: phases in global memory (large data)
                     L.cmc_set_config(R, T, ph)
                     try:
                         cfg = job.config()

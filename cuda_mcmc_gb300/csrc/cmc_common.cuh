@@ -138,6 +138,8 @@ struct Cta {
   float *scratch;
   int ist[R];                       // global replica index of each local replica
   int tid, nthreads;
+  int ph_region;                    // first of R consecutive per-replica regions of a
+                                    // global model scratch (disjoint between CTAs)
 };
 
 template <class Model, int R>

@@ -37,6 +37,7 @@ eval_kernel(const cmc_job job, const typename Model::Packed pk, int mode)
   cta.nthreads = T;
 #pragma unroll
   for (int r = 0; r < R; ++r) cta.ist[r] = blockIdx.x * R + r;
+  cta.ph_region = blockIdx.x * R;
 
   for (int i = tid; i < R * nptot; i += T) {
     int r = i / nptot, j = i - r * nptot;

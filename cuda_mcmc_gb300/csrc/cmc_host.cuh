@@ -102,6 +102,15 @@ size_t plan_bytes(const cmc_job &j, const typename Model::Packed &pk, int R, int
                    Model::scratch_bytes(pk, R)).total;
 }
 
+// Phase mode 2 (global memory) is available: the model supports it and the
+// job's work holds the regions (Model::host_dims set the pointer).
+template <class Model>
+inline bool global_phases_ok(const typename Model::Packed &pk)
+{
+  if constexpr (Model::kGlobalPhases) return pk.gph != nullptr;
+  else return false;
+}
+
 // Pick replicas-per-CTA R (cluster size G = nbeta/R <= 16), threads T and the
 // phase storage mode.  Score = waves * R, proportional to the makespan when
 // every cluster carries the same work; ties go to the smaller R.
@@ -126,8 +135,9 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
     for (int T : Ts) {
       if (Tfix && T != Tfix) continue;
       if (!Tfix && T == 64 && R > 4) continue;
-      for (int ph = 1; ph >= 0; --ph) {
+      for (int ph = 2; ph >= 0; --ph) {
         if (Pfix >= 0 && ph != Pfix) continue;
+        if (ph == 2 && !global_phases_ok<Model>(pk)) continue;
         typename Model::Packed q = pk;
         q.phasor = ph;
         const size_t smem = plan_bytes<Model>(j, q, R, T, 1);
@@ -142,7 +152,9 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         // phasors once the phasors cost co-residency
         const int tpr = T / R;
         const double shape = (tpr == 32) ? 1.0 : (tpr == 64 || tpr == 16) ? 1.1 : 1.25;
-        const double score = (double)waves * R * (ph ? 1.0 : 1.02) * shape;
+        // phases in global memory cost an L2 round trip per closure gather
+        const double store = (ph == 1) ? 1.0 : (ph == 0) ? 1.02 : 1.08;
+        const double score = (double)waves * R * store * shape;
         if (score < best - 1e-9) {
           best = score;
           out.R = R; out.G = G; out.T = T; out.phasor = ph; out.smem = smem;
@@ -208,8 +220,9 @@ int run_sweep(const cmc_job &j, cudaStream_t s, LaunchCfg *used = nullptr)
   const char *err = nullptr;
   rc = Model::host_dims(j, 0, pk, &err);
   if (rc) return fail(rc, err);
-  if (Model::host_work_bytes(pk) > 0 && (j.work == nullptr || j.work_bytes < Model::host_work_bytes(pk)))
-    return fail(CMC_ERR_ARG, "job.work is smaller than cmc_work_bytes()");
+  if (Model::host_work_bytes_min(pk) > 0 &&
+      (j.work == nullptr || j.work_bytes < Model::host_work_bytes_min(pk)))
+    return fail(CMC_ERR_ARG, "job.work is smaller than the packed data (cmc_work_bytes())");
   LaunchCfg c;
   rc = pick_sweep_config<Model>(j, pk, c);
   if (rc) return rc;
@@ -231,8 +244,9 @@ int run_eval(const cmc_job &j, int mode, cudaStream_t s)
   const char *err = nullptr;
   rc = Model::host_dims(j, mode, pk, &err);
   if (rc) return fail(rc, err);
-  if (Model::host_work_bytes(pk) > 0 && (j.work == nullptr || j.work_bytes < Model::host_work_bytes(pk)))
-    return fail(CMC_ERR_ARG, "job.work is smaller than cmc_work_bytes()");
+  if (Model::host_work_bytes_min(pk) > 0 &&
+      (j.work == nullptr || j.work_bytes < Model::host_work_bytes_min(pk)))
+    return fail(CMC_ERR_ARG, "job.work is smaller than the packed data (cmc_work_bytes())");
   pk.phasor = 0;
   const int lim = smem_optin();
   const int T = 128;
@@ -244,7 +258,17 @@ int run_eval(const cmc_job &j, int mode, cudaStream_t s)
     smem = plan_bytes<Model>(j, pk, r, T, 0);
     if ((long long)smem <= lim) { R = r; break; }
   }
-  if (!R) return fail(CMC_ERR_UNSUPPORTED, "one replica's model rows do not fit in shared memory");
+  if (!R && global_phases_ok<Model>(pk)) {   // phases in global memory
+    pk.phasor = 2;
+    for (int r : Rs) {
+      if (r > Model::kMaxR) continue;
+      smem = plan_bytes<Model>(j, pk, r, T, 0);
+      if ((long long)smem <= lim) { R = r; break; }
+    }
+  }
+  if (!R)
+    return fail(CMC_ERR_UNSUPPORTED, "one replica's model rows do not fit in shared memory "
+                                     "(give job.work cmc_work_bytes() bytes for larger data)");
   rc = Model::host_pack(j, pk, j.work, s);
   if (rc) return fail(rc, "packing the model data failed");
   return dispatch_R<Model>(R, [&](auto rcnst) {
@@ -259,6 +283,17 @@ size_t work_bytes(const cmc_job &j, int mode)
   const char *err = nullptr;
   if (Model::host_dims(j, mode, pk, &err)) return 0;
   return Model::host_work_bytes(pk);
+}
+
+// The smallest job.work a launch accepts: the packed data alone (no global
+// phase regions).
+template <class Model>
+size_t work_bytes_min(const cmc_job &j, int mode)
+{
+  typename Model::Packed pk;
+  const char *err = nullptr;
+  if (Model::host_dims(j, mode, pk, &err)) return 0;
+  return Model::host_work_bytes_min(pk);
 }
 
 // ---- batches of independent jobs (fits) ------------------------------------
@@ -327,7 +362,7 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
       fail(rc, err);
       break;
     }
-    const size_t wb = Model::host_work_bytes(pk[i]);
+    const size_t wb = Model::host_work_bytes_min(pk[i]);
     if (wb > 0 && (v.work == nullptr || v.work_bytes < wb)) {
       rc = fail(CMC_ERR_ARG, "batch: a job's work is smaller than cmc_work_bytes()");
       break;
@@ -364,6 +399,8 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
     double best = -1.0;
     long long reps = 0;
     for (int i : mem) reps += (long long)jobs[i].nseq * nbeta;
+    bool gl_all = true;   // every job of the class can keep its phases in global memory
+    for (int i : mem) gl_all = gl_all && global_phases_ok<Model>(pk[i]);
     const int Rs[] = {1, 2, 4, 8, 16, 32};
     for (int R : Rs) {
       if (R > Model::kMaxR || nbeta % R || nbeta / R > 16) continue;
@@ -372,7 +409,8 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
       // points of the class's largest job
       const int want = std::max(32 * R, (int)std::min<long long>(256, Model::points(pk[big]) / 16));
       const int T = want <= 64 ? 64 : want <= 128 ? 128 : 256;
-      for (int ph = 1; ph >= 0; --ph) {
+      for (int ph = 2; ph >= 0; --ph) {
+        if (ph == 2 && !gl_all) continue;
         Packed q = pk[big];
         q.phasor = ph;
         const size_t smem = plan_bytes<Model>(jobs[big], q, R, T, 1);
@@ -382,7 +420,9 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
         });
         if (cap <= 0) continue;
         const double resident = std::min((double)cap * nbeta, (double)reps);
-        const double score = resident * (ph ? 1.05 : 1.0);
+        // per resident replica: phasors > phases in shared memory > phases in
+        // global memory (an L2 round trip per closure gather)
+        const double score = resident * (ph == 1 ? 1.05 : ph == 0 ? 1.0 : 0.95);
         if (score > best + 1e-9) {
           best = score;
           bc.R = R; bc.G = G; bc.T = T; bc.phasor = ph; bc.smem = smem; bc.nclusters = cap;

@@ -68,6 +68,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   cta.nthreads = T;
 #pragma unroll
   for (int r = 0; r < R; ++r) cta.ist[r] = (rank * R + r) * nseq + iseq;
+  cta.ph_region = iseq * nbeta + rank * R;
 
   // ---- load tables and state -------------------------------------------
   for (int i = tid; i < nprm; i += T) s_ivar[i] = job.ivar[i];

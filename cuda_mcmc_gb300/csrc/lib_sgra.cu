@@ -41,7 +41,7 @@ extern "C" int cmc_run_noalloc(const cmc_job *job, void *stream)
 {
   cmc::last_error().clear();
   if (!job) return cmc::fail(CMC_ERR_ARG, "cmc_run_noalloc: job is NULL");
-  const size_t need = cmc::work_bytes<cmc::SgraModel>(*job, 0);
+  const size_t need = cmc::work_bytes_min<cmc::SgraModel>(*job, 0);
   if (need > kStaticWorkBytes)
     return cmc::fail(CMC_ERR_ARG,
                      "cmc_run_noalloc: the packed data needs " + std::to_string(need) +
@@ -82,7 +82,7 @@ extern "C" int cmc_run_noalloc(const cmc_job *job, void *stream)
 namespace {
 size_t grad_extra_offset(const cmc::SgraModel::Packed &pk)
 {
-  return (cmc::SgraModel::host_work_bytes(pk) + 255) & ~(size_t)255;
+  return cmc::SgraModel::host_work_bytes_min(pk);
 }
 
 int grad_dims(const cmc_job &j, cmc::SgraModel::Packed &pk)

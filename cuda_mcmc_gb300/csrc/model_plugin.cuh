@@ -52,6 +52,8 @@ struct PluginModel {
   }
 
   static size_t host_work_bytes(const Packed &) { return 0; }
+  static size_t host_work_bytes_min(const Packed &) { return 0; }
+  static constexpr bool kGlobalPhases = false;
 
   static int host_pack(const cmc_job &, Packed &, void *, cudaStream_t) { return CMC_OK; }
 

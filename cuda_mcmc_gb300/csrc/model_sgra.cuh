@@ -108,8 +108,18 @@ struct SgraModel {
     const int *orig;     // [npts] index of vis[i] in the caller's order
     const int4 *cli;     // [ncph] sorted-point indices i, j, k of closure c
     const float4 *clf;   // [ncph] cos obs, sin obs, 1/sigma^2, obs
-    int nvis, npts, ncph, cpext, npass, imodel, phasor, ndat;
+    float *gph;          // [nrep][npts] phases in global memory (phasor == 2), or null
+    int nvis, npts, ncph, cpext, npass, imodel, phasor, ndat, nrep;
   };
+
+  // Phase storage (Packed::phasor): 1 = unit phasors in shared memory, 0 =
+  // phases in shared memory, 2 = phases in global memory (L2), one npts-long
+  // region per replica in job.work after the packed data.  Mode 2 frees the
+  // shared memory that large data sets need for their phases, so that more
+  // replicas per CTA and more CTAs per SM fit; it is offered from
+  // kGlobalPhaseMinPts points on and when job.work holds the regions.
+  static constexpr bool kGlobalPhases = true;
+  static constexpr int kGlobalPhaseMinPts = 2048;
 
   static constexpr bool kRowsInEval = false;
   static constexpr int kMaxR = 8;   // instantiated replicas-per-CTA counts: 1, 2, 4, 8
@@ -119,10 +129,21 @@ struct SgraModel {
   // data points one replica's evaluation runs over
   __host__ __device__ static int points(const Packed &pk) { return pk.npts + pk.ncph; }
 
-  // shared scratch: Bessel table, then phasors [R][npts] (float2) or phases (float)
+  // shared scratch: Bessel table, then phasors [R][npts] (float2) or phases
+  // (float); the table only when the phases live in global memory
   __host__ __device__ static unsigned scratch_bytes(const Packed &pk, int R)
   {
+    if (pk.phasor == 2) return kTabBytes;
     return kTabBytes + (unsigned)R * (unsigned)pk.npts * (pk.phasor ? 8u : 4u);
+  }
+
+  // the phases of local replica 0 of a CTA (replica r at + r * npts)
+  template <class Cta>
+  __device__ static float *phase_area(const Cta &cta)
+  {
+    const Packed &pk = *cta.pk;
+    if (pk.phasor == 2) return pk.gph + (size_t)cta.ph_region * pk.npts;
+    return cta.scratch + kTabBytes / 4;
   }
 
   // ---- host side: sizes, validation, packing ------------------------------
@@ -139,6 +160,8 @@ struct SgraModel {
     if (pk.npass < 2) pk.ncph = 0;   // closures are a pass-1 product
     pk.npts = pk.nvis + (pk.cpext ? 3 * pk.ncph : 0);
     pk.phasor = 1;
+    pk.nrep = nrep;
+    pk.gph = nullptr;
     if (j.nidat < 1 || pk.nvis < 0 || pk.nvis > j.ndat) {
       *err = "Sgr A* model: idat[0] (nvis) must be in [0, ndat]";
       return CMC_ERR_ARG;
@@ -166,12 +189,27 @@ struct SgraModel {
              "head plus the phase tail)";
       return CMC_ERR_ARG;
     }
+    if (pk.npts >= kGlobalPhaseMinPts && j.work != nullptr &&
+        j.work_bytes >= host_work_bytes(pk))
+      pk.gph = reinterpret_cast<float *>(static_cast<unsigned char *>(j.work) +
+                                         host_work_bytes_min(pk));
     return CMC_OK;
   }
 
+  // the packed data (what every launch needs), 256-byte aligned
+  static size_t host_work_bytes_min(const Packed &pk)
+  {
+    const size_t b = (size_t)pk.npts * 48 + (size_t)pk.ncph * 32 + 256;
+    return (b + 255) & ~(size_t)255;
+  }
+
+  // packed data + the global phase regions when the data set is large enough
+  // to use them (cmc_work_bytes reports this size)
   static size_t host_work_bytes(const Packed &pk)
   {
-    return (size_t)pk.npts * 48 + (size_t)pk.ncph * 32 + 256;
+    size_t b = host_work_bytes_min(pk);
+    if (pk.npts >= kGlobalPhaseMinPts) b += (size_t)pk.nrep * pk.npts * sizeof(float);
+    return b;
   }
 
   static int host_pack(const cmc_job &j, Packed &pk, void *work, cudaStream_t s);
@@ -263,22 +301,26 @@ struct SgraModel {
     bool big = false;
 #pragma unroll
     for (int r = 0; r < R; ++r) big |= (cta.flag[r] != 0 && cta.consts[r].bigx != 0);
-    if (cta.pk->phasor) {
-      if (big) eval_impl<R, true, true>(cta, acc);
-      else eval_impl<R, true, false>(cta, acc);
+    if (cta.pk->phasor == 1) {
+      if (big) eval_impl<R, true, true, false>(cta, acc);
+      else eval_impl<R, true, false, false>(cta, acc);
+    } else if (cta.pk->phasor == 0) {
+      if (big) eval_impl<R, false, true, false>(cta, acc);
+      else eval_impl<R, false, false, false>(cta, acc);
     } else {
-      if (big) eval_impl<R, false, true>(cta, acc);
-      else eval_impl<R, false, false>(cta, acc);
+      if (big) eval_impl<R, false, true, true>(cta, acc);
+      else eval_impl<R, false, false, true>(cta, acc);
     }
   }
 
-  template <int R, bool PH, bool BIG, class Cta>
+  // PH: unit phasors (else phases); GL: phases in global memory.
+  template <int R, bool PH, bool BIG, bool GL, class Cta>
   __device__ static void eval_impl(Cta &cta, float (&acc)[R])
   {
     const Packed &pk = *cta.pk;
     const int tid = cta.tid, T = cta.nthreads, npts = pk.npts;
     const float4 *btab = reinterpret_cast<const float4 *>(cta.scratch);
-    float *zs = cta.scratch + kTabBytes / 4;
+    float *zs = GL ? pk.gph + (size_t)cta.ph_region * npts : cta.scratch + kTabBytes / 4;
     float2 *z = reinterpret_cast<float2 *>(zs);
     bool act[R];
 #pragma unroll
@@ -306,7 +348,7 @@ struct SgraModel {
       }
     }
     if (pk.ncph == 0 || pk.npass < 2) return;
-    __syncthreads();
+    __syncthreads();   // also orders the global phase stores before the reads (GL)
     for (int c = tid; c < pk.ncph; c += T) {
       const int4 q = __ldg(&pk.cli[c]);
       const float4 f = __ldg(&pk.clf[c]);
@@ -371,7 +413,7 @@ struct SgraModel {
     const int tid = cta.tid, T = cta.nthreads, npts = pk.npts, nvis = pk.nvis;
     const int ndat = pk.ndat, nptot = job.nptot;
     const size_t nchi2m = (size_t)job.nbeta * job.nseq * ndat;
-    float *ph = cta.scratch + kTabBytes / 4;   // phases [R][npts]
+    float *ph = phase_area(cta);               // phases [R][npts]
     __syncthreads();
     if (tid < R && evald[tid]) prepare(cta, tid, plast + tid * nptot);
     __syncthreads();

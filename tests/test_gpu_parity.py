@@ -317,3 +317,37 @@ def test_errors_are_reported_not_faults():
     job3.job.nbeta = 1
     with pytest.raises(_lib.McmcError, match="nbeta"):
         job3.run(1, 1, do_init=True)
+
+
+def test_global_memory_phases_equal_shared_memory_phases():
+    """Phase storage mode 2 (per-replica phases in global memory, for large
+    data sets) stores the same float phases as mode 0 (shared memory): a
+    run in each mode with the same R and T gives bit-identical results."""
+    w = synth.sgra(nvis=3000, ncph=900, seed=31, nseq=4, nbeta=8)
+    out = []
+    for ph in (0, 2):
+        job = DeviceJob.from_workload(w, niter_total=6, seed=5)
+        job.shape = {"R": 4, "T": 128, "phasor": ph}
+        assert job.config()["phasor"] == ph
+        job.run(4, 0, do_init=True)
+        job.run(0, 6)
+        job.check()
+        out.append(job.to_numpy())
+    for k in ("pout", "tout", "chi2", "pcur", "chi2c", "pstp", "n_acpt", "n_exch", "rndst",
+              "datm", "chi2m"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_calc_modchi2_beyond_shared_memory_uses_global_phases():
+    """60,000 visibilities: one replica's phases (240 KB) exceed shared
+    memory; with cmc_work_bytes() of scratch the evaluation keeps them in
+    global memory and matches the FP64 oracle."""
+    w = synth.sgra(nvis=60000, ncph=2000, seed=32, nseq=1, nbeta=2)
+    job = DeviceJob.from_workload(w, niter_total=1, seed=5)
+    P = np.stack([w.truth, w.truth * np.float32(1.02)])[:, None, :].astype(np.float32)
+    job.set_state(pcur=P, flag=np.ones((2, 1), np.int32))
+    job.eval()
+    job.check()
+    s = job.to_numpy(("chi2c",))
+    _, _, _, c64 = oracle.calc_modchi2(_pb(w), P.reshape(2, -1))
+    assert np.max(np.abs(s["chi2c"].ravel() - c64) / c64) < CHI2_RTOL
