@@ -541,8 +541,9 @@ def run_ess_batch(args, rank, world, local):
     """ESS per second over many independent fits: the plain per-fit form (one
     cmc_run per fit, the reference's proposals) against the fused form (all
     fits in persistent work-list launches; after a quarter of the burn-in,
-    polish + Fisher information + restart + block proposals), same fits,
-    replicas and iteration budget."""
+    polish + Fisher information + restart + block proposals, and the rest of
+    the sweep replayed as one captured CUDA graph), same fits, replicas and
+    iteration budget."""
     import torch
     from cuda_mcmc_gb300 import fit, synth
     from cuda_mcmc_gb300.device import BatchJob, DeviceJob
@@ -569,8 +570,8 @@ def run_ess_batch(args, rank, world, local):
         for j, o in zip(jobs, objs):
             fit.fisher_setup(j, o)
         b = BatchJob(jobs)            # descriptors now carry the block proposals
-        b.run(nb - n1, 0)
-        b.run(0, ni, itr0=0)
+        g = b.graph_schedule(nb - n1, ni, chunk=250)   # the rest of the sweep: one graph
+        g.replay()
 
     def timed(fn, jobs):
         torch.cuda.synchronize()

@@ -331,6 +331,29 @@ class BatchJob:
             self.run(nburn, niter, itr0=itr0, stream=side)
         return g
 
+    def graph_schedule(self, nburn, niter, chunk=256, itr0=0):
+        """Capture a whole sweep schedule as ONE CUDA graph: nburn burn-in
+        iterations, then niter recorded ones (columns itr0 ..), each phase as
+        launches of at most ``chunk`` iterations (so a replay can be followed
+        chunk by chunk with events, and no launch runs for long).  Replaying
+        the graph once runs the schedule from the jobs' current state."""
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.graph(g, stream=side):
+            done = 0
+            while done < nburn:
+                n = min(chunk, nburn - done)
+                self.run(n, 0, itr0=itr0, stream=side)
+                done += n
+            done = 0
+            while done < niter:
+                n = min(chunk, niter - done)
+                self.run(0, n, itr0=itr0 + done, stream=side)
+                done += n
+        self.itr_done = itr0 + niter
+        return g
+
     def classes(self):
         out = []
         n = self.L.cmc_batch_info(self.plan, -1, None, None, None, None, None, None, None)

@@ -72,3 +72,28 @@ def test_batch_rejects_mixed_nbeta():
     b = DeviceJob.from_workload(synth.sgra(nvis=100, ncph=30, nseq=2, nbeta=16), niter_total=1)
     with pytest.raises(_lib.McmcError, match="nbeta"):
         BatchJob([a, b])
+
+
+def test_graph_schedule_equals_direct_launches():
+    """BatchJob.graph_schedule captures burn-in and recorded chunks in one
+    CUDA graph; one replay equals the same launches issued directly."""
+    fits = _fits()[:2]
+    nburn, niter = 7, 9
+    outs = []
+    for use_graph in (False, True):
+        jobs = [DeviceJob.from_workload(w, niter_total=niter, seed=40 + i)
+                for i, w in enumerate(fits)]
+        b = BatchJob(jobs)
+        b.run(0, 0, do_init=True)
+        if use_graph:
+            b.graph_schedule(nburn, niter, chunk=4).replay()
+        else:
+            for n in (4, 3):
+                b.run(n, 0)
+            for i0, n in ((0, 4), (4, 4), (8, 1)):
+                b.run(0, n, itr0=i0)
+        b.check()
+        outs.append([j.to_numpy() for j in jobs])
+    for a, c in zip(*outs):
+        for k in ("pout", "tout", "chi2", "pcur", "chi2c", "rndst", "pstp"):
+            assert np.array_equal(a[k], c[k]), k
