@@ -55,10 +55,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="use the library's heuristic shape")
-    ap.add_argument("--workload", default="sgra", choices=["sgra", "batch", "ess", "ess-batch"],
+    ap.add_argument("--workload", default="sgra",
+                    choices=["sgra", "batch", "ess", "ess-batch", "rosenbrock", "nlsys"],
                     help="sgra: one 64x32 Sgr A* fit; batch: many independent fits; "
                          "ess: ESS/sec of Fisher block proposals vs the reference's proposals; "
-                         "ess-batch: the same over many fits, batched vs one fit per launch")
+                         "ess-batch: the same over many fits, batched vs one fit per launch; "
+                         "rosenbrock / nlsys: the plugin-model configurations, one full run "
+                         "per step")
     ap.add_argument("--nfits", type=int, default=1024)
     ap.add_argument("--ess-burn", type=int, default=2000)
     ap.add_argument("--ess-iter", type=int, default=4000)
@@ -394,11 +397,19 @@ def run_mine(args, rank, world, local):
         threads = os.cpu_count() or 1
         cev, cdt = CpuSweep(w, threads, 1).step(1)
         r = cev / cdt
+        # the same sweep on one core: 4 of the sequences, 1 iteration
+        import copy
+        w1 = copy.copy(w)
+        w1.nseq = 4
+        c1, d1 = CpuSweep(w1, 1, 1).step(1)
         line["cpu_baseline"] = {"value": r, "unit": "chi2 evals/s", "cores": threads,
                                 "kind": "port",
                                 "sample": "1 iteration x %d replicas (%d evals, %.1f s), oracle "
                                           "sweep with FP64 model, sequences over %d threads" % (
-                                              w.nseq * w.nbeta, cev, cdt, threads)}
+                                              w.nseq * w.nbeta, cev, cdt, threads),
+                                "one_core": {"value": c1 / d1, "cores": 1,
+                                             "sample": "1 iteration x %d replicas (%d evals)" % (
+                                                 w1.nseq * w1.nbeta, c1)}}
     print(json.dumps(line))
 
 
@@ -416,6 +427,12 @@ def run_batch(args, rank, world, local):
     batch = BatchJob(jobs)
     batch.run(0, 0, do_init=True)
     batch.check()
+    heuristic = batch.classes()
+    tune_s = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        batch.autotune(iters=1)
+        tune_s = time.perf_counter() - t0
     g = batch.graph(nb, ni, itr0=0)
     for _ in range(args.warmup):
         g.replay()
@@ -457,6 +474,7 @@ def run_batch(args, rank, world, local):
                                "16x16 replicas each (%d data in total)" % (len(fits), terms),
                    "step": "%d burn-in + %d main iterations of every fit" % (nb, ni),
                    "parallelism": "replicas only", "classes": batch.classes(),
+                   "heuristic_classes": heuristic, "autotune_s": tune_s,
                    "l2": "inputs larger than L2 in total"},
         "roofline": {"bound": "fp32", "achieved": fl * args.steps / dt / 1e12, "peak": peak,
                      "unit": "TFLOP/s", "frac": fl * args.steps / dt / 1e12 / peak,
@@ -629,6 +647,53 @@ def run_ess_batch(args, rank, world, local):
     print(json.dumps(line))
 
 
+def run_plugin(args, rank, world, local):
+    """The plugin-model configurations (Rosenbrock N=4: 16 x 32, 1000 + 5000
+    iterations; the 8-unknown nonlinear system: 64 x 32, 2000 + 10000), a step
+    being one complete run (init + burn-in + recorded iterations) of the
+    config, beside the oracle port of the same sweep on the host cores."""
+    import torch
+    from cuda_mcmc_gb300 import synth
+    from cuda_mcmc_gb300.device import DeviceJob
+    w = synth.rosenbrock() if args.workload == "rosenbrock" else synth.nlsys()
+    job = DeviceJob.from_workload(w, niter_total=w.niter, seed=1234 + rank)
+    evals = (w.nburn + w.niter) * w.nprm * w.nbeta * w.nseq
+    for _ in range(args.warmup):
+        job.run(w.nburn, w.niter, do_init=True, itr0=0)
+    job.check()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            job.run(w.nburn, w.niter, do_init=True, itr0=0)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    job.check()
+    dt = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    cev, cdt = CpuSweep(w, threads, 20).step(20)
+    line = {
+        "metric": "chi2 model evals/sec", "value": evals * args.steps * world / dt,
+        "unit": "chi2 evals/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "%s, %dx%d replicas, %d + %d iterations" % (
+            w.name, w.nseq, w.nbeta, w.nburn, w.niter), "launch": job.config(),
+            "step": "one complete run (%d chi2 evals)" % evals},
+        "cpu_baseline": {"value": cev / cdt, "unit": "chi2 evals/s", "cores": threads,
+                         "kind": "port", "sample": "20 iterations of all replicas (%d evals)" % cev},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args)
@@ -638,6 +703,8 @@ def main():
         run_ess(args, rank, world, local)
     elif args.impl == "mine" and args.workload == "ess-batch":
         run_ess_batch(args, rank, world, local)
+    elif args.impl == "mine" and args.workload in ("rosenbrock", "nlsys"):
+        run_plugin(args, rank, world, local)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -72,7 +72,8 @@ EXPORTS = ("mcmc_cuda", "mcmc_cuda_v2", "calc_modchi2", "calc_modchi2_v2", "calc
            "calc_model_v2", "cmc_last_error", "cmc_model_name", "cmc_abi_version",
            "cmc_sizeof_job", "cmc_reset_gpu", "cmc_work_bytes", "cmc_run", "cmc_eval",
            "cmc_query_config", "cmc_set_config", "cmc_batch_work_bytes", "cmc_batch_prepare",
-           "cmc_batch_run", "cmc_batch_info", "cmc_batch_free")
+           "cmc_batch_run", "cmc_batch_info", "cmc_batch_free", "cmc_batch_run_class",
+           "cmc_batch_set_class")
 
 
 def _declare(L):
@@ -116,6 +117,12 @@ def _declare(L):
     L.cmc_batch_info.restype = C.c_int
     L.cmc_batch_free.argtypes = [C.c_void_p]
     L.cmc_batch_free.restype = None
+    L.cmc_batch_run_class.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_void_p]
+    L.cmc_batch_run_class.restype = C.c_int
+    L.cmc_batch_set_class.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_void_p]
+    L.cmc_batch_set_class.restype = C.c_int
     if hasattr(L, "cmc_grad"):          # Sgr A* library only
         L.cmc_grad_work_bytes.argtypes = [C.POINTER(CmcJob)]
         L.cmc_grad_work_bytes.restype = C.c_size_t

@@ -39,6 +39,12 @@ constexpr int kRepF = 4;         // per-replica floats: ptent, chi2c, chi2n, bet
 constexpr int kRepI = 4;         // per-replica ints: ptentn, flag, kchosen, evaluated
 constexpr int kMaxRetry = 64;    // bound on the k-redraw loops (u == 1.0 exactly)
 
+// Angle wrapped into [-pi, pi] as the reference does (atan2(sin, cos),
+// src/gpu_mcmc.cu:389-393).  Out of line: one compiled body shared by every
+// kernel and call site of a translation unit, so that the sweep and batch
+// kernels round it identically whatever the compiler does around the call.
+static __device__ __noinline__ float wrap_pi(float p) { return atan2f(sinf(p), cosf(p)); }
+
 __device__ __forceinline__ void set_status(int *st, int code)
 {
   if (st) atomicCAS(st, 0, code);

@@ -495,6 +495,70 @@ int batch_run(BatchPlan *P, int do_init, int nburn, int niter, int itr0, cudaStr
   return CMC_OK;
 }
 
+// Launches of one class only (the autotuner times classes one by one).
+template <class Model>
+int batch_run_class(BatchPlan *P, int cls, int do_init, int nburn, int niter, int itr0,
+                    cudaStream_t s)
+{
+  using Packed = typename Model::Packed;
+  if (!P) return fail(CMC_ERR_ARG, "batch: plan is NULL");
+  if (cls < 0 || cls >= (int)P->classes.size()) return fail(CMC_ERR_ARG, "batch: no such class");
+  if (nburn < 0 || niter < 0 || itr0 < 0 || itr0 + niter > P->min_niter_total)
+    return fail(CMC_ERR_ARG, "batch: need nburn, niter >= 0 and itr0 + niter <= niter_total");
+  const BatchClass &bc = P->classes[cls];
+  CMC_CUDA(cudaMemsetAsync(P->counters_dev + cls, 0, sizeof(int), s));
+  return dispatch_R<Model>(bc.R, [&](auto rcn) {
+    return launch_batch<Model, decltype(rcn)::value>(
+        P->jobs_dev, reinterpret_cast<const Packed *>(P->pks_dev), P->items_dev + bc.item0,
+        bc.nitems, P->counters_dev + cls, bc.G, bc.T, bc.smem, bc.nclusters, do_init, nburn,
+        niter, itr0, s);
+  });
+}
+
+// Give class `cls` the launch shape (R, T, phase mode) if every job of the
+// class fits it; the jobs' descriptors are re-uploaded on `s` (synchronised).
+template <class Model>
+int batch_set_class(BatchPlan *P, int cls, int R, int T, int phasor, cudaStream_t s)
+{
+  using Packed = typename Model::Packed;
+  if (!P) return fail(CMC_ERR_ARG, "batch: plan is NULL");
+  if (cls < 0 || cls >= (int)P->classes.size()) return fail(CMC_ERR_ARG, "batch: no such class");
+  const int nbeta = P->jobs[0].nbeta;
+  if (R < 1 || R > Model::kMaxR || nbeta % R != 0 || nbeta / R > 16)
+    return fail(CMC_ERR_UNSUPPORTED, "batch: R must divide nbeta with nbeta/R <= 16");
+  if ((T != 64 && T != 128 && T != 256) || T < 32 * ((R + 31) / 32))
+    return fail(CMC_ERR_UNSUPPORTED, "batch: T must be 64, 128 or 256 and >= 32 per 32 replicas");
+  if (phasor < 0 || phasor > 2) return fail(CMC_ERR_ARG, "batch: phase mode must be 0, 1 or 2");
+  BatchClass &bc = P->classes[cls];
+  Packed *pk = reinterpret_cast<Packed *>(P->pks.data());
+  std::vector<int> mem;
+  for (int it = bc.item0; it < bc.item0 + bc.nitems; ++it) {
+    const int j = P->items[it].x;
+    if (mem.empty() || mem.back() != j) mem.push_back(j);
+  }
+  size_t smem = 0;
+  for (int i : mem) {
+    if (phasor == 2 && !global_phases_ok<Model>(pk[i]))
+      return fail(CMC_ERR_UNSUPPORTED, "batch: a job of the class has no global phase regions");
+    Packed q = pk[i];
+    q.phasor = phasor;
+    smem = std::max(smem, plan_bytes<Model>(P->jobs[i], q, R, T, 1));
+  }
+  if ((long long)smem > smem_optin())
+    return fail(CMC_ERR_UNSUPPORTED, "batch: the class's shared memory does not fit this shape");
+  const int G = nbeta / R;
+  const int cap = dispatch_R<Model>(R, [&](auto rcn) {
+    return batch_capacity<Model, decltype(rcn)::value>(G, T, smem);
+  });
+  if (cap <= 0) return fail(CMC_ERR_UNSUPPORTED, "batch: no cluster of this shape is resident");
+  bc.R = R; bc.G = G; bc.T = T; bc.phasor = phasor; bc.smem = smem;
+  bc.nclusters = std::min(cap, bc.nitems);
+  for (int i : mem) pk[i].phasor = phasor;
+  CMC_CUDA(cudaMemcpyAsync(P->pks_dev, P->pks.data(), P->pks.size(), cudaMemcpyHostToDevice, s));
+  CMC_CUDA(cudaStreamSynchronize(s));
+  return CMC_OK;
+}
+
 // ---- the reference's host-pointer entry points ------------------------------
 
 // One device allocation carved into 256-byte aligned pieces.

@@ -157,7 +157,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
         int k = s_ivar[i];
         float u = rng.uniform();
         float p = __fmaf_rn(s_pmax[k] - s_pmin[k], u, s_pmin[k]);
-        if (s_pdescr[k] == 2) p = atan2f(sinf(p), cosf(p));
+        if (s_pdescr[k] == 2) p = wrap_pi(p);
         params[r * nptot + k] = p;
       }
       for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
@@ -246,7 +246,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
     for (int i = 0; i < nprm; ++i) {
       const int t = s_ivar[i];
       float p = __fmaf_rn(sd, acc[i], blk[r * nptot + t]);
-      if (s_pdescr[t] == 2) p = atan2f(sinf(p), cosf(p));
+      if (s_pdescr[t] == 2) p = wrap_pi(p);
       out |= (p < s_pmin[t]) || (p > s_pmax[t]);
       params[r * nptot + t] = p;
     }
@@ -284,7 +284,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
           const float sd = s_pstp[r * nprm + k];
           const float rn = rng.normal();
           p = __fmaf_rn(sd, rn, p);
-          if (s_pdescr[t] == 2) p = atan2f(sinf(p), cosf(p));
+          if (s_pdescr[t] == 2) p = wrap_pi(p);
           if ((p < s_pmin[t]) || (p > s_pmax[t])) {
             s_flag[r] = 0;
           } else {

@@ -41,6 +41,15 @@ __device__ __forceinline__ void sincospi_mufu(float t, float *s, float *c)
   *c = sg * __cosf(x);
 }
 
+// sin(x), cos(x) as sin / cos(pi t), t = x / pi, from the polynomials above:
+// rint, multiplies and explicit fmaf only, so that every kernel and call site
+// rounds it identically (the per-proposal constants of the sweep and batch
+// kernels must agree to the bit).  A few float32 ulps for |x| up to ~10^3.
+__device__ __forceinline__ void sincos_fma(float x, float *s, float *c)
+{
+  sincospi_poly(x * 0.318309886183790672f, s, c);
+}
+
 #ifndef CMC_MUFU_SINCOS
 #define CMC_MUFU_SINCOS 1
 #endif

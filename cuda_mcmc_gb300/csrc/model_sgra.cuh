@@ -225,6 +225,8 @@ struct SgraModel {
   template <class Cta>
   __device__ static void after_exchange(Cta &) {}
 
+  // Its sines and cosines use sincos_fma (explicit FMAs only): the init and
+  // proposal paths of the sweep and batch kernels must round them the same.
   template <class Cta>
   __device__ static void prepare(Cta &cta, int r, const float *p)
   {
@@ -242,11 +244,15 @@ struct SgraModel {
     const float Rex = (pi / 180.0f) * (Re / 3600.0f) * 1e3f;   // uas -> nrad
     const float Rin = rq * Rex;
     float d = ecc * (Rex - Rin);
-    if (im != 1) d *= cosf(eta - th);
+    if (im != 1) {
+      float se, ce;
+      sincos_fma(eta - th, &se, &ce);
+      d *= ce;
+    }
     const float h = (2.0f / pi) / fmaf(fmaf(-(Rin * Rin), 1.0f + d / Rex, Rex * Rex), fade,
                                        fmaf(-(Rin * Rin), 1.0f - d / Rex, Rex * Rex));
     const float h0 = fade * h;
-    sincosf(th, &c.sth, &c.cth);
+    sincos_fma(th, &c.sth, &c.cth);
     c.kex = 2.0f * pi * Rex;
     c.kin = 2.0f * pi * Rin;
     c.ae = 0.5f * (h + h0) * Rex * c.kex;
@@ -269,8 +275,8 @@ struct SgraModel {
       c.gpv = -2.0f * gshift * c.sth;
     } else {
       float sa, ca;
-      sincosf(beta, &c.gs, &c.gc);
-      sincosf(alpha, &sa, &ca);
+      sincos_fma(beta, &c.gs, &c.gc);
+      sincos_fma(alpha, &sa, &ca);
       c.gpu = -2.0f * gr * Rex * ca;
       c.gpv = -2.0f * gr * Rex * sa;
     }

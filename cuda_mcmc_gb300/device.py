@@ -354,6 +354,69 @@ class BatchJob:
         self.itr_done = itr0 + niter
         return g
 
+    def run_class(self, cls, nburn=0, niter=0, itr0=0, stream=None):
+        """Launch size class ``cls`` alone (burn-in / recorded iterations)."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(self.L, self.L.cmc_batch_run_class(self.plan, int(cls), 0, int(nburn),
+                                                      int(niter), int(itr0),
+                                                      C.c_void_p(s.cuda_stream)))
+
+    def set_class(self, cls, R, T, phasor, stream=None):
+        """Give class ``cls`` the shape (R, T, phasor); raises McmcError if a
+        job of the class does not fit it."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(self.L, self.L.cmc_batch_set_class(self.plan, int(cls), int(R), int(T),
+                                                      int(phasor), C.c_void_p(s.cuda_stream)))
+
+    def autotune(self, iters=2, R_values=(1, 2, 4, 8, 16, 32), T_values=(64, 128, 256),
+                 verbose=False):
+        """Time every feasible shape of every size class on the batch itself
+        (``iters`` burn-in iterations of the class, from a saved state that is
+        restored after each trial) and keep the fastest per class.  Returns
+        the chosen shapes."""
+        saved_fields = ("pcur", "chi2c", "flag", "ptent", "ptentn", "pstp", "n_acpt", "n_exch",
+                        "n_cnt", "n_hist", "tcur", "rndst", "datm", "chi2m", "status")
+        saved = [{k: j.t[k].clone() for k in saved_fields} for j in self.jobs]
+
+        def restore():
+            for j, sv in zip(self.jobs, saved):
+                for k, v in sv.items():
+                    j.t[k].copy_(v)
+
+        chosen = []
+        try:
+            for c, cur in enumerate(self.classes()):
+                best, best_t = (cur["R"], cur["T"], cur["phasor"]), float("inf")
+                for R in R_values:
+                    for T in T_values:
+                        for ph in (1, 0, 2):
+                            try:
+                                self.set_class(c, R, T, ph)
+                            except _lib.McmcError:
+                                continue
+                            times = []
+                            for _ in range(2):          # the first run loads the instance
+                                e0 = torch.cuda.Event(enable_timing=True)
+                                e1 = torch.cuda.Event(enable_timing=True)
+                                e0.record()
+                                self.run_class(c, nburn=iters)
+                                e1.record()
+                                e1.synchronize()
+                                times.append(e0.elapsed_time(e1))
+                                restore()
+                            if verbose:
+                                print("class %d R=%d T=%d phasor=%d: %.3f ms" % (c, R, T, ph,
+                                                                                times[-1]))
+                            if times[-1] < best_t:
+                                best_t, best = times[-1], (R, T, ph)
+                self.set_class(c, *best)
+                chosen.append(dict(zip(("R", "T", "phasor"), best), ms=best_t))
+        finally:
+            restore()
+            torch.cuda.synchronize(self.device)
+        self.check()
+        return chosen
+
     def classes(self):
         out = []
         n = self.L.cmc_batch_info(self.plan, -1, None, None, None, None, None, None, None)

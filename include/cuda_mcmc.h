@@ -148,13 +148,21 @@ int cmc_fisher(const cmc_job *job, float *fisher, void *stream);
  * from an atomic counter, with this launch's iteration window (do_init, nburn,
  * niter, itr0) applied to every job; it can be captured in a CUDA graph.
  * cmc_batch_info reports class `cls`'s launch shape (returns the number of
- * classes); cmc_batch_free releases the host-side plan. */
+ * classes); cmc_batch_free releases the host-side plan.
+ * cmc_batch_set_class gives class `cls` another launch shape (R replicas per
+ * CTA, T threads, phase mode 0/1/2) when every job of the class fits it, and
+ * re-uploads the descriptors (synchronising `stream`); cmc_batch_run_class
+ * launches that class alone.  Together they let a caller time the shapes of
+ * each class (cuda_mcmc_gb300.device.BatchJob.autotune). */
 size_t cmc_batch_work_bytes(const cmc_job *jobs, int njobs);
 void *cmc_batch_prepare(const cmc_job *jobs, int njobs, void *work, size_t work_bytes,
                         void *stream);
 int cmc_batch_run(void *plan, int do_init, int nburn, int niter, int itr0, void *stream);
 int cmc_batch_info(void *plan, int cls, int *R, int *G, int *T, int *phasor, int *nitems,
                    int *nclusters, size_t *smem);
+int cmc_batch_run_class(void *plan, int cls, int do_init, int nburn, int niter, int itr0,
+                        void *stream);
+int cmc_batch_set_class(void *plan, int cls, int R, int T, int phasor, void *stream);
 void cmc_batch_free(void *plan);
 
 /* Bytes of library scratch (packed data of the built-in fast models) that

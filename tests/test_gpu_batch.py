@@ -97,3 +97,47 @@ def test_graph_schedule_equals_direct_launches():
     for a, c in zip(*outs):
         for k in ("pout", "tout", "chi2", "pcur", "chi2c", "rndst", "pstp"):
             assert np.array_equal(a[k], c[k]), k
+
+
+def test_autotune_restores_state_and_keeps_chains_exact():
+    """BatchJob.autotune times the shapes of each class on the batch itself
+    and restores the state after every trial; the tuned batch still walks each
+    fit's single-job chain with the chosen class shape, bit for bit."""
+    fits = _fits()
+    nburn, niter = 4, 5
+    jobs = [DeviceJob.from_workload(w, niter_total=niter, seed=500 + i) for i, w in enumerate(fits)]
+    batch = BatchJob(jobs)
+    batch.run(0, 0, do_init=True)
+    batch.check()
+    before = [j.to_numpy() for j in jobs]
+    chosen = batch.autotune(iters=1, R_values=(2, 4, 8), T_values=(128, 256))
+    after = [j.to_numpy() for j in jobs]
+    for a, b in zip(before, after):
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
+    classes = batch.classes()
+    assert [(c["R"], c["T"], c["phasor"]) for c in classes] == \
+        [(c["R"], c["T"], c["phasor"]) for c in chosen]
+    batch.run(0, 0, do_init=True)     # restart with the tuned shapes from the first chi^2
+    batch.run(nburn, 0)
+    batch.run(0, niter)
+    batch.check()
+    for i, w in enumerate(fits):
+        got = jobs[i].to_numpy()
+        ok = False
+        for c in classes:
+            ref = DeviceJob.from_workload(w, niter_total=niter, seed=500 + i)
+            ref.shape = {"R": c["R"], "T": c["T"], "phasor": c["phasor"]}
+            try:
+                ref.run(0, 0, do_init=True)
+                ref.run(nburn, 0)
+                ref.run(0, niter)
+                ref.check()
+            except _lib.McmcError:
+                continue
+            r = ref.to_numpy()
+            if all(np.array_equal(r[k], got[k]) for k in ("pout", "chi2", "pcur", "chi2c",
+                                                           "rndst")):
+                ok = True
+                break
+        assert ok, "fit %d matched no tuned class shape" % i
