@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "cmc_job.h"
 #include "fastmath.cuh"
@@ -87,12 +88,13 @@ __device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, const float4 *bt
 // Data packing kernels (defined once, in the library translation unit).
 __global__ void sgra_points_kernel(const float *coor, const float *dat, const float *std2r,
                                    int nvis, int ncph, int cpext, float4 *raw, float *key);
-__global__ void rank_kernel(const float *key, int n, int *newpos);
+__global__ void sgra_mark_kernel(const int *icoor, int nvis, int ncph, int cpext, int *used);
+__global__ void rank_kernel(const float *key, const int *used, int n, int *newpos);
 __global__ void sgra_scatter_kernel(const float4 *raw, const float *key, const int *newpos,
-                                    int npts, const int *icoor, const float *dat,
-                                    const float *std2r, int nvis, int ncph, int cpext,
-                                    float4 *vis, float *rho, int *orig, int4 *cli, float4 *clf,
-                                    int *status);
+                                    const int *used, int npts, const int *icoor,
+                                    const float *dat, const float *std2r, int nvis, int ncph,
+                                    int cpext, float4 *vis, float *rho, int *orig, int4 *cli,
+                                    float4 *clf, int *aux, int *status);
 
 // CMC_BRANCHFREE: evaluate every local replica and drop the terms of the
 // inactive ones, so that the R independent evaluations interleave.
@@ -109,6 +111,8 @@ struct SgraModel {
     const int4 *cli;     // [ncph] sorted-point indices i, j, k of closure c
     const float4 *clf;   // [ncph] cos obs, sin obs, 1/sigma^2, obs
     float *gph;          // [nrep][npts] phases in global memory (phasor == 2), or null
+    const int *aux;      // [0]: nused -- points [0, nused) are closure corners and need a
+                         // phase; [1]: max |uv| (float bits)
     int nvis, npts, ncph, cpext, npass, imodel, phasor, ndat, nrep;
   };
 
@@ -162,6 +166,7 @@ struct SgraModel {
     pk.phasor = 1;
     pk.nrep = nrep;
     pk.gph = nullptr;
+    pk.aux = nullptr;
     if (j.nidat < 1 || pk.nvis < 0 || pk.nvis > j.ndat) {
       *err = "Sgr A* model: idat[0] (nvis) must be in [0, ndat]";
       return CMC_ERR_ARG;
@@ -199,7 +204,7 @@ struct SgraModel {
   // the packed data (what every launch needs), 256-byte aligned
   static size_t host_work_bytes_min(const Packed &pk)
   {
-    const size_t b = (size_t)pk.npts * 48 + (size_t)pk.ncph * 32 + 256;
+    const size_t b = (size_t)pk.npts * 52 + (size_t)pk.ncph * 32 + 512;
     return (b + 255) & ~(size_t)255;
   }
 
@@ -294,7 +299,7 @@ struct SgraModel {
       c.gauss = !(gax == 0.0f || aq == 0.0f);
     }
     if (!c.gauss) c.zg = 0.0f;
-    const float rho_max = (cta.pk->npts > 0) ? cta.pk->rho[cta.pk->npts - 1] : 0.0f;
+    const float rho_max = (cta.pk->npts > 0) ? __int_as_float(__ldg(&cta.pk->aux[1])) : 0.0f;
     c.bigx = !(fmaxf(fabsf(c.kex), fabsf(c.kin)) * rho_max < (float)kBesselIntervals);
   }
 
@@ -334,7 +339,10 @@ struct SgraModel {
       acc[r] = 0.0f;
       act[r] = cta.flag[r] != 0;
     }
-    for (int i = tid; i < npts; i += T) {
+    // One model term per (point, replica); the points are packed closure
+    // corners first, so only the first nused need a phase: each thread walks
+    // its stride through [0, nused) with phases, then on without.
+    auto terms = [&](int i, auto with_phase) {
       const float4 d = __ldg(&pk.vis[i]);
       const float rho = __ldg(&pk.rho[i]);
 #pragma unroll
@@ -347,12 +355,19 @@ struct SgraModel {
         const float rs = (n2 > 0.0f) ? rsqrtf(n2) : 0.0f;
         const float dif = fmaf(-n2, rs, d.z);
         acc[r] = fmaf(act[r] ? dif * dif : 0.0f, d.w, acc[r]);
-        if (PH)
-          z[r * npts + i] = (n2 > 0.0f) ? make_float2(V.x * rs, V.y * rs) : make_float2(1.f, 0.f);
-        else
-          zs[r * npts + i] = atan2_poly(V.y, V.x);
+        if constexpr (decltype(with_phase)::value) {
+          if (PH)
+            z[r * npts + i] = (n2 > 0.0f) ? make_float2(V.x * rs, V.y * rs)
+                                          : make_float2(1.f, 0.f);
+          else
+            zs[r * npts + i] = atan2_poly(V.y, V.x);
+        }
       }
-    }
+    };
+    const int nused = (pk.ncph > 0 && pk.npass >= 2) ? __ldg(&pk.aux[0]) : 0;
+    int i = tid;
+    for (; i < nused; i += T) terms(i, std::true_type{});
+    for (; i < npts; i += T) terms(i, std::false_type{});
     if (pk.ncph == 0 || pk.npass < 2) return;
     __syncthreads();   // also orders the global phase stores before the reads (GL)
     for (int c = tid; c < pk.ncph; c += T) {
@@ -492,22 +507,45 @@ __global__ void sgra_points_kernel(const float *coor, const float *dat, const fl
   }
 }
 
-// newpos[i] = rank of (key[i], i) in lexicographic order: a deterministic
-// total order, so the packing is identical from run to run.
-__global__ void rank_kernel(const float *key, int n, int *newpos)
+// used[p] = 1 for every point a closure phase reads: the three visibilities
+// of each triangle (cpExt = 0) or the triangle corners (cpExt = 1).
+// Out-of-range indices are skipped here (the scatter reports them).
+__global__ void sgra_mark_kernel(const int *icoor, int nvis, int ncph, int cpext, int *used)
+{
+  const int npts = nvis + (cpext ? 3 * ncph : 0);
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncph; c += gridDim.x * blockDim.x) {
+    if (cpext) {
+      used[nvis + 3 * c] = used[nvis + 3 * c + 1] = used[nvis + 3 * c + 2] = 1;
+    } else {
+      for (int t = 0; t < 3; ++t) {
+        const int a = icoor[3 * c + t];
+        if (a >= 0 && a < npts) used[a] = 1;
+      }
+    }
+  }
+}
+
+// newpos[i] = rank of (!used[i], key[i], i) in lexicographic order: closure
+// corners first, each group by |uv|; a deterministic total order, so the
+// packing is identical from run to run.
+__global__ void rank_kernel(const float *key, const int *used, int n, int *newpos)
 {
   __shared__ float tile[256];
+  __shared__ int utile[256];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const float ki = (i < n) ? key[i] : 0.0f;
+  const int ui = (i < n && used[i]) ? 0 : 1;
   int cnt = 0;
   for (int base = 0; base < n; base += 256) {
     const int j = base + threadIdx.x;
     tile[threadIdx.x] = (j < n) ? key[j] : 0.0f;
+    utile[threadIdx.x] = (j < n && used[j]) ? 0 : 1;
     __syncthreads();
     const int m = min(256, n - base);
     for (int t = 0; t < m; ++t) {
       const float kj = tile[t];
-      cnt += (kj < ki) || (kj == ki && base + t < i);
+      const int uj = utile[t];
+      cnt += (uj < ui) || (uj == ui && ((kj < ki) || (kj == ki && base + t < i)));
     }
     __syncthreads();
   }
@@ -515,10 +553,10 @@ __global__ void rank_kernel(const float *key, int n, int *newpos)
 }
 
 __global__ void sgra_scatter_kernel(const float4 *raw, const float *key, const int *newpos,
-                                    int npts, const int *icoor, const float *dat,
-                                    const float *std2r, int nvis, int ncph, int cpext,
-                                    float4 *vis, float *rho, int *orig, int4 *cli, float4 *clf,
-                                    int *status)
+                                    const int *used, int npts, const int *icoor,
+                                    const float *dat, const float *std2r, int nvis, int ncph,
+                                    int cpext, float4 *vis, float *rho, int *orig, int4 *cli,
+                                    float4 *clf, int *aux, int *status)
 {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npts + ncph;
        i += gridDim.x * blockDim.x) {
@@ -527,6 +565,8 @@ __global__ void sgra_scatter_kernel(const float4 *raw, const float *key, const i
       vis[p] = raw[i];
       rho[p] = key[i];
       orig[p] = i;
+      if (used[i]) atomicAdd(&aux[0], 1);
+      atomicMax(&aux[1], __float_as_int(key[i]));   // keys are >= 0 (or +inf)
     } else {
       const int c = i - npts;
       int a, b, e;
@@ -561,16 +601,23 @@ int SgraModel::host_pack(const cmc_job &j, Packed &pk, void *work, cudaStream_t 
   float4 *clf = (float4 *)(w + o); o += al(16 * nc);
   float4 *raw = (float4 *)(w + o); o += al(16 * n);
   float *key = (float *)(w + o);   o += al(4 * n);
-  int *newpos = (int *)(w + o);
-  pk.vis = vis; pk.rho = rho; pk.orig = orig; pk.cli = cli; pk.clf = clf;
+  int *newpos = (int *)(w + o);    o += al(4 * n);
+  int *used = (int *)(w + o);      o += al(4 * n);
+  int *aux = (int *)(w + o);
+  pk.vis = vis; pk.rho = rho; pk.orig = orig; pk.cli = cli; pk.clf = clf; pk.aux = aux;
+  if (cudaMemsetAsync(aux, 0, 4 * sizeof(int), s) != cudaSuccess) return CMC_ERR_CUDA;
   if (n == 0) return CMC_OK;
+  if (cudaMemsetAsync(used, 0, 4 * n, s) != cudaSuccess) return CMC_ERR_CUDA;
   const int blocks = (int)std::min<size_t>((n + nc + 255) / 256, 4096);
   sgra_points_kernel<<<blocks, 256, 0, s>>>(j.coor, j.dat, j.std2r, pk.nvis, pk.ncph, pk.cpext,
                                             raw, key);
-  rank_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(key, (int)n, newpos);
-  sgra_scatter_kernel<<<blocks, 256, 0, s>>>(raw, key, newpos, (int)n, j.icoor, j.dat, j.std2r,
-                                             pk.nvis, pk.ncph, pk.cpext, vis, rho, orig, cli,
-                                             clf, j.status);
+  if (nc > 0)
+    sgra_mark_kernel<<<(unsigned)std::min<size_t>((nc + 255) / 256, 4096), 256, 0, s>>>(
+        j.icoor, pk.nvis, pk.ncph, pk.cpext, used);
+  rank_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(key, used, (int)n, newpos);
+  sgra_scatter_kernel<<<blocks, 256, 0, s>>>(raw, key, newpos, used, (int)n, j.icoor, j.dat,
+                                             j.std2r, pk.nvis, pk.ncph, pk.cpext, vis, rho, orig,
+                                             cli, clf, aux, j.status);
   return cudaGetLastError() == cudaSuccess ? CMC_OK : CMC_ERR_CUDA;
 }
 #endif  // CMC_INSTANCE_TU
