@@ -141,3 +141,22 @@ def test_autotune_restores_state_and_keeps_chains_exact():
                 ok = True
                 break
         assert ok, "fit %d matched no tuned class shape" % i
+
+
+def test_plugin_model_batch_finds_the_rosenbrock_minimum():
+    """A batch of plugin-model fits (Rosenbrock N=4, the reference's
+    search_Rosenbrock example) runs through the same persistent launches and
+    each fit's best recorded sample lies in the minimum's valley: f(x) < 0.02
+    and within 0.2 of (1, 1, 1, 1) (the valley is flat along its curve)."""
+    fits = [synth.rosenbrock(n=4, nseq=16, nbeta=32, nburn=1000, niter=2000) for _ in range(3)]
+    jobs = [DeviceJob.from_workload(w, niter_total=2000, seed=900 + i) for i, w in enumerate(fits)]
+    batch = BatchJob(jobs)
+    batch.run(1000, 0, do_init=True)
+    batch.run(0, 2000)
+    batch.check()
+    for j in jobs:
+        s = j.to_numpy()
+        i = np.argmin(s["chi2"])
+        x = s["pout"][:, 0].reshape(4, -1)[:, i].astype(np.float64)
+        f = np.sum(100 * (x[1:] - x[:-1] ** 2) ** 2 + (1 - x[:-1]) ** 2)
+        assert f < 0.02 and np.all(np.abs(x - 1.0) < 0.2), (x, f)

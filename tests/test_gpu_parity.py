@@ -156,13 +156,35 @@ def _oracle_state_from(job_state, w, niter_total):
     return st
 
 
-@pytest.mark.parametrize("cfg", ["sgra", "nlsys", "rosenbrock"])
+def _sgra_cpext(w, seed=12):
+    """The workload's visibilities with its closures given as triangle
+    corners (cpExt = 1): u1, v1, u2, v2 per closure, the third corner
+    -(u1 + u2), -(v1 + v2)."""
+    import dataclasses
+    rng = np.random.default_rng(seed)
+    nvis, ncph = int(w.idat[0]), w.ndat - int(w.idat[0])
+    corners = rng.uniform(-6, 6, (ncph, 4)).astype(np.float32)
+    return dataclasses.replace(
+        w, coor=np.concatenate([w.coor[:2 * nvis], corners.ravel()]).astype(np.float32),
+        dat=np.concatenate([w.dat[:nvis], rng.uniform(-3, 3, ncph)]).astype(np.float32),
+        std2r=np.concatenate([w.std2r[:nvis], np.full(ncph, 100.0)]).astype(np.float32),
+        icoor=np.zeros(1, np.int32), idat=np.array([nvis, 0, 1], np.int32))
+
+
+@pytest.mark.parametrize("cfg", ["sgra", "sgra_cpext", "sgra_npass1", "nlsys", "rosenbrock"])
 def test_sweep_lockstep_vs_fp64_oracle(cfg):
     """Larger data than the fixtures: from the same state and the same
     injected draws, every iteration of the kernel makes the FP64 oracle's
-    decisions (near ties excepted) and reaches its chi^2 within 1e-5."""
+    decisions (near ties excepted) and reaches its chi^2 within 1e-5.
+    Sgr A* with closures from visibility triplets, from triangle corners
+    (cpExt = 1) and without the closure pass (npass = 1)."""
+    import dataclasses
     if cfg == "sgra":
         w = synth.sgra(nvis=400, ncph=120, seed=8, nseq=2, nbeta=8)
+    elif cfg == "sgra_cpext":
+        w = _sgra_cpext(synth.sgra(nvis=400, ncph=120, seed=8, nseq=2, nbeta=8))
+    elif cfg == "sgra_npass1":
+        w = dataclasses.replace(synth.sgra(nvis=400, ncph=120, seed=8, nseq=2, nbeta=8), npass=1)
     elif cfg == "nlsys":
         w = synth.nlsys(nseq=2, nbeta=8)
     else:
