@@ -119,3 +119,88 @@ def test_sgra_fit_from_uv_file(tmp_path):
     mamp, mph = m.calcmodel(U, V, p, imodel=1, uv_layout="interleaved")
     a, ph = oracle.sgra_vis(1, p, U.ravel(), V.ravel())
     assert np.max(np.abs(mamp.ravel() - a) - 1e-5 * a) <= 1e-6 * p[0]
+
+
+@pytest.mark.gpu
+def test_search_rosenbrock_api_example_replay():
+    """examples/search_Rosenbrock/search_Rosenbrock_api.py:60-160 (compute
+    section, Python 3): the arrays built as the example builds them, one
+    mcmc_interf.mcmcuda call on the Rosenbrock plugin, and the example's
+    result -- the minimum chi^2 sample at (1, 1)."""
+    from cuda_mcmc_gb300 import mcmc_interf as mi
+    from numpy import array, float32, int32, uint8, uint64, where, zeros, ones_like, arange
+    nseq, nbeta, niter, nburn = int32(14), int32(32), int32(1000), int32(400)
+    seed = uint64(12345)
+    imodel = 0
+    pdescr = array((1, 1), dtype=int32)
+    ptotal = array((0., 0.), dtype=float32)
+    nptot = len(ptotal)
+    pmint = array((-5., -5.), dtype=float32)
+    pmaxt = array((5., 5.), dtype=float32)
+    ivar = where(pdescr != 0)[0].astype(int32)
+    nprm = len(ivar)
+    pmin, pmax = pmint[ivar], pmaxt[ivar]
+    invar = zeros(nptot, dtype=int32)
+    ip = 0
+    for i in range(nptot):
+        if pdescr[i] != 0:
+            invar[i] = ip
+            ip = ip + 1
+        else:
+            invar[i] = -1
+    nadj = int32(100)
+    beta1, betan = float32(1.), float32(0.0001)
+    npass = 1
+    coor = array((2, 2, 0.25, 0.5), dtype=float32); ncoor = len(coor)
+    icoor = zeros(1, dtype=int32); nicoor = len(coor)      # the example's over-read
+    dat = zeros(1, dtype=float32); ndat = len(dat)
+    std2r = ones_like(dat, dtype=float32)
+    idat = zeros(1, dtype=int32); nidat = len(idat)
+    datm = zeros((nbeta * nseq * ndat), dtype=float32); ndatm = len(datm)
+    chi2m = zeros((nbeta, nseq, ndat), dtype=float32)
+    rndst = zeros((nbeta, nseq, 48), dtype=uint8)
+    beta = zeros((nbeta), dtype=float32)
+    pstp = zeros((nprm, nbeta, nseq), dtype=float32)
+    pout = zeros((nprm, nbeta, nseq, niter), dtype=float32)
+    tout = zeros((nbeta, nseq, niter), dtype=int32)
+    chi2 = zeros((nseq, niter), dtype=float32)
+    flag = zeros((nbeta, nseq), dtype=int32)
+    tcur = zeros((nbeta, nseq), dtype=int32)
+    chi2c = zeros((nbeta, nseq), dtype=float32)
+    n_cnt = zeros((nprm, nbeta, nseq), dtype=int32)
+    n_acpt = zeros((nprm, nbeta, nseq), dtype=int32)
+    n_exch = zeros((nbeta, nseq), dtype=int32)
+    n_hist = zeros((nadj, nprm, nbeta, nseq), dtype=int32)
+    ptentn = zeros((nbeta, nseq), dtype=int32)
+    ptent = zeros((nbeta, nseq), dtype=float32)
+    pcur = zeros((nbeta, nseq, nptot), dtype=float32)
+    for i in range(nbeta):
+        for j in range(nseq):
+            pcur[i, j, :] = ptotal
+            for k in range(nprm):
+                pcur[i, j, ivar[k]] = pmin[k] + (pmax[k] - pmin[k]) / 2.
+    pmid = (pmax - pmin) / 50.
+    for i in range(nprm):
+        pstp[i, :, :] = pmid[i]
+    n0_nbeta = arange(nbeta)
+    for i in range(nseq):
+        tcur[:, i] = n0_nbeta
+    bstp = (betan / beta1) ** (1.0 / float(nbeta - 1))
+    for i in range(nbeta):
+        beta[i] = beta1 * bstp ** i
+    n_cnt[:] = float32(1.)
+    mi.use_model("rosenbrock")
+    with pytest.warns(RuntimeWarning, match="zero-padded"):
+        mi.mcmcuda(coor, dat, std2r, icoor, idat, datm, chi2m, pdescr, ivar, invar, ptotal,
+                   pmint, pmaxt, pout, tout, chi2, chi2c, tcur, flag, n_acpt, n_exch, n_cnt,
+                   n_hist, beta, pstp, ptent, ptentn, pcur, rndst, uint64(seed), int32(imodel),
+                   int32(ncoor), int32(ndat), int32(nicoor), int32(nidat), int32(ndatm),
+                   int32(nptot), int32(nprm), int32(nadj), int32(npass), int32(nbeta),
+                   int32(nseq), int32(nburn), int32(niter))
+    mi.reset_gpu()
+    mi.use_model("sgra")
+    c2 = chi2.flatten()
+    po = pout[:, 0, :, :].reshape((nprm, nseq * niter))
+    im = c2.argmin()
+    assert np.all(np.abs(po[:, im] - 1.0) < 0.05), po[:, im]
+    assert (c2 < 0.00001).sum() > 0
