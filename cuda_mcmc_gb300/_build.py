@@ -50,6 +50,8 @@ def _sources_digest(extra=()):
     h = hashlib.sha1(os.environ.get("CMC_NVCC_FLAGS", "").encode())
     for d in (CSRC, INCLUDE):
         for name in sorted(os.listdir(d)):
+            if not os.path.isfile(os.path.join(d, name)):
+                continue
             with open(os.path.join(d, name), "rb") as f:
                 h.update(name.encode())
                 h.update(f.read())

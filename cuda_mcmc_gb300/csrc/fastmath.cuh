@@ -81,17 +81,19 @@ __device__ __forceinline__ float atan2_poly(float y, float x)
 }
 
 // F1(x) = J1(x)/x and F2(x) = J2(x)/x^2 (even in x) from the piecewise
-// polynomial table `tab` (a shared-memory copy of kBesselTab: per interval,
-// (kBesselDeg + 1) / 2 float4 of coefficient pairs).  BIG = false: x is known
-// to lie inside the table (straight-line code); BIG = true: beyond the table
-// F1, F2 come from CUDA's j0f/j1f with J2 = 2 J1/x - J0.
+// polynomial table `tab` (a shared-memory copy of kBesselTab: per interval of
+// width 1/kBesselSub, (kBesselDeg + 1) / 2 float4 of coefficient pairs, in
+// t = kBesselSub x - (i + 0.5)).  BIG = false: x is known to lie inside the
+// table (straight-line code); BIG = true: beyond the table F1, F2 come from
+// CUDA's j0f/j1f with J2 = 2 J1/x - J0.
 template <bool BIG>
 __device__ __forceinline__ void bessel_f12_tab(const float4 *tab, float x, float &f1, float &f2)
 {
   constexpr int kQ = (kBesselDeg + 1) / 2;
   x = fabsf(x);
-  const int i = min((int)x, kBesselIntervals - 1);
-  const float d = x - ((float)i + 0.5f);
+  const float xs = x * (float)kBesselSub;
+  const int i = min((int)xs, kBesselIntervals - 1);
+  const float d = xs - ((float)i + 0.5f);
   const float4 *c = tab + i * kQ;
   float4 a = c[kQ - 1];
   float p1 = fmaf(a.z, d, a.x), p2 = fmaf(a.w, d, a.y);
@@ -103,7 +105,7 @@ __device__ __forceinline__ void bessel_f12_tab(const float4 *tab, float x, float
   }
   f1 = p1;
   f2 = p2;
-  if (BIG && x >= (float)kBesselIntervals) {
+  if (BIG && x >= (float)kBesselXmax) {
     const float ix = 1.0f / x;
     const float j0 = j0f(x), j1 = j1f(x);
     f1 = j1 * ix;

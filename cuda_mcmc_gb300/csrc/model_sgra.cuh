@@ -300,7 +300,7 @@ struct SgraModel {
     }
     if (!c.gauss) c.zg = 0.0f;
     const float rho_max = (cta.pk->npts > 0) ? __int_as_float(__ldg(&cta.pk->aux[1])) : 0.0f;
-    c.bigx = !(fmaxf(fabsf(c.kex), fabsf(c.kin)) * rho_max < (float)kBesselIntervals);
+    c.bigx = !(fmaxf(fabsf(c.kex), fabsf(c.kin)) * rho_max < (float)kBesselXmax);
   }
 
   // chi^2 of every active replica over all data (both passes).  The phase

@@ -142,9 +142,10 @@ __device__ void sgra_consts_t(const S *p, int im, S (&c)[kNC], int &inner, int &
 __device__ __forceinline__ float bessel_f3_tab(const float *tab3, float x)
 {
   x = fabsf(x);
-  if (x < (float)kBesselIntervals) {
-    const int i = (int)x;
-    const float d = x - ((float)i + 0.5f);
+  if (x < (float)kBesselXmax) {
+    const float xs = x * (float)kBesselSub;
+    const int i = min((int)xs, kBesselIntervals - 1);
+    const float d = xs - ((float)i + 0.5f);
     const float *c = tab3 + i * (kBesselDeg + 1);
     float p = c[kBesselDeg];
 #pragma unroll
