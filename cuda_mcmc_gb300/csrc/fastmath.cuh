@@ -29,16 +29,16 @@ __device__ __forceinline__ void sincospi_poly(float t, float *s, float *c)
   *c = sg * pc;
 }
 
-// sin(pi t), cos(pi t) from the hardware approximations: t is reduced to
-// r = t - rint(t) in [-1/2, 1/2] first, where __sinf / __cosf have an
-// absolute error below 2^-21.4.
+// sin(pi t), cos(pi t) from the hardware approximations (MUFU.SIN / COS)
+// applied to pi t directly: their absolute error stays below 2^-20.5 for
+// |pi t| <= 100 pi (PTX ISA, sin.approx / cos.approx), and the model's
+// arguments stay within a few pi (|t| = |2 d U| or |Gaussian offset * uv| of
+// a few units), so no explicit range reduction is needed.
 __device__ __forceinline__ void sincospi_mufu(float t, float *s, float *c)
 {
-  const float n = rintf(t);
-  const float x = (t - n) * 3.14159265358979324f;
-  const float sg = (((int)n) & 1) ? -1.0f : 1.0f;
-  *s = sg * __sinf(x);
-  *c = sg * __cosf(x);
+  const float x = t * 3.14159265358979324f;
+  *s = __sinf(x);
+  *c = __cosf(x);
 }
 
 // sin(x), cos(x) as sin / cos(pi t), t = x / pi, from the polynomials above:
