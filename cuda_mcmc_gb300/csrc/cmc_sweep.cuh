@@ -307,12 +307,15 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
 
     // ---- replica_exchange (src/gpu_mcmc.cu:533-626) ------------------------
     cluster.sync();
-    if (rank == 0 && tid == 0) {
-      for (int s = 0; s < nbeta; ++s) {
-        const float *rc = cluster.map_shared_rank(s_chi2c, s / R);
-        x_chi2[s] = rc[s % R];
+    if (rank == 0) {
+      // gather the nbeta chi^2 values in parallel (one remote load each)
+      for (int s = tid; s < nbeta; s += T) {
+        x_chi2[s] = cluster.map_shared_rank(s_chi2c, s / R)[s % R];
         x_perm[s] = s;
       }
+      __syncthreads();
+    }
+    if (rank == 0 && tid == 0) {
       const int nb1 = nbeta - 1;
       for (int ib = 0; ib < nbeta; ++ib) {
         const int k = rng.index(nb1, job.status);

@@ -246,25 +246,31 @@ struct SgraModel {
       gr = p[5]; gax = p[6]; aq = p[7]; gq = p[8];
       alpha = p[9]; beta = p[10]; eta = p[11]; th = p[12];
     }
-    const float Rex = (pi / 180.0f) * (Re / 3600.0f) * 1e3f;   // uas -> nrad
-    const float Rin = rq * Rex;
-    float d = ecc * (Rex - Rin);
+    // Two divisions in all (1/Rex and h): this runs on one thread per replica
+    // between the evaluations, so its latency is paid once per proposal.
+    // Products that feed a sum are __fmul_rn (never contracted), so the sweep
+    // and batch kernels round them identically.
+    const float Rex = Re * 4.84813681109536e-3f;   // uas -> nrad: (pi/180)/3600*1e3
+    const float Rin = __fmul_rn(rq, Rex);
+    float d = __fmul_rn(ecc, Rex - Rin);
     if (im != 1) {
       float se, ce;
       sincos_fma(eta - th, &se, &ce);
-      d *= ce;
+      d = __fmul_rn(d, ce);
     }
-    const float h = (2.0f / pi) / fmaf(fmaf(-(Rin * Rin), 1.0f + d / Rex, Rex * Rex), fade,
-                                       fmaf(-(Rin * Rin), 1.0f - d / Rex, Rex * Rex));
-    const float h0 = fade * h;
+    const float dr = __fmul_rn(d, 1.0f / Rex);
+    const float h = (2.0f / pi) / fmaf(fmaf(-(Rin * Rin), 1.0f + dr, Rex * Rex), fade,
+                                       fmaf(-(Rin * Rin), 1.0f - dr, Rex * Rex));
+    const float h0 = __fmul_rn(fade, h);
+    const float hm = (h - h0) * (-0.25f / pi);      // -(h - h0) / (4 pi)
     sincos_fma(th, &c.sth, &c.cth);
     c.kex = 2.0f * pi * Rex;
     c.kin = 2.0f * pi * Rin;
     c.ae = 0.5f * (h + h0) * Rex * c.kex;
-    c.be = -(h - h0) / (4.0f * pi) * (c.kex * c.kex * c.kex);
+    c.be = hm * (c.kex * c.kex * c.kex);
     c.inner = (Rin != 0.0f);
-    c.ai = c.inner ? 0.5f * (h + h0 - d * (h - h0) / Rex) * Rin * c.kin : 0.0f;
-    c.bi = c.inner ? -(h - h0) / (4.0f * pi) * rq * (c.kin * c.kin * c.kin) : 0.0f;
+    c.ai = c.inner ? 0.5f * fmaf(-dr, h - h0, h + h0) * Rin * c.kin : 0.0f;
+    c.bi = c.inner ? hm * rq * (c.kin * c.kin * c.kin) : 0.0f;
     c.dsh = 2.0f * d;
     // 2 (pi / (2 sqrt(2 ln 2)))^2 = pi^2 / (4 ln 2): FWHM^2 -> Gaussian exponent
     const float gcoef = 3.5597039f;
