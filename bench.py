@@ -280,14 +280,26 @@ def e2e_rate(w, args, steps, warmup):
     s0 = sampler_defaults(w.pdescr, w.pmint, w.pmaxt, w.nbeta, w.nseq)
     beta = w.beta()
 
+    # host buffers in pinned (page-locked) memory, allocated once: every step
+    # copies its inputs from them and its results back into them
+    tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.int32): torch.int32,
+           np.dtype(np.uint8): torch.uint8}
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=tdt[np.dtype(dtype)], pin_memory=True).numpy()
+
+    sp = {k: pinned(v.shape, v.dtype) for k, v in s0.items()}
+    pout = pinned((nprm, w.nbeta, w.nseq, ni), np.float32)
+    tout = pinned((w.nbeta, w.nseq, ni), np.int32)
+    chi2 = pinned((w.nseq, ni), np.float32)
+    datm = pinned((nrep * (w.ndat + w.nvis),), np.float32)
+    chi2m = pinned((w.nbeta, w.nseq, w.ndat), np.float32)
+    rndst = pinned((w.nbeta, w.nseq, 48), np.uint8)
+
     def call(seed):
-        s = {k: v.copy() for k, v in s0.items()}
-        pout = np.empty((nprm, w.nbeta, w.nseq, ni), np.float32)
-        tout = np.empty((w.nbeta, w.nseq, ni), np.int32)
-        chi2 = np.empty((w.nseq, ni), np.float32)
-        datm = np.zeros(nrep * (w.ndat + w.nvis), np.float32)
-        chi2m = np.zeros((w.nbeta, w.nseq, w.ndat), np.float32)
-        rndst = np.zeros((w.nbeta, w.nseq, 48), np.uint8)
+        for k, v in s0.items():        # the step's starting state
+            sp[k][...] = v
+        s = sp
         mcmc_interf.mcmcuda(w.coor, w.dat, w.std2r, w.icoor, w.idat, datm, chi2m, s["pdescr"],
                             s["ivar"], s["invar"], s["ptotal"], s["pmint"], s["pmaxt"], pout,
                             tout, chi2, s["chi2c"], s["tcur"], s["flag"], s["n_acpt"],
