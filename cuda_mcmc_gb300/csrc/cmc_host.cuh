@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -112,8 +113,7 @@ inline bool global_phases_ok(const typename Model::Packed &pk)
 }
 
 // Pick replicas-per-CTA R (cluster size G = nbeta/R <= 16), threads T and the
-// phase storage mode.  Score = waves * R, proportional to the makespan when
-// every cluster carries the same work; ties go to the smaller R.
+// phase storage mode by the ranking below (autotune.py measures instead).
 template <class Model>
 int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &out)
 {
@@ -147,14 +147,16 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         });
         if (n <= 0) continue;
         const int waves = (j.nseq + n - 1) / n;
-        // makespan ~ waves * R; measured on GB300 (Sgr A*, 2600 data):
-        // about 32 threads per replica beats 16 or 64, and phases beat
-        // phasors once the phasors cost co-residency
+        // Measured on GB300 (Sgr A*, 2000-20000 visibilities): fewest waves
+        // of resident clusters first; then about 32 threads per replica
+        // (16 or 64 cost ~10 %); then the phase storage (phasors, phases in
+        // shared memory, phases in global memory: an L2 round trip per
+        // closure gather); then more replicas per CTA (more independent
+        // work per thread).  Lexicographic, lower is better.
         const int tpr = T / R;
-        const double shape = (tpr == 32) ? 1.0 : (tpr == 64 || tpr == 16) ? 1.1 : 1.25;
-        // phases in global memory cost an L2 round trip per closure gather
-        const double store = (ph == 1) ? 1.0 : (ph == 0) ? 1.02 : 1.08;
-        const double score = (double)waves * R * store * shape;
+        const int shape_rank = (tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2;
+        const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
+        const double score = waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 - R;
         if (score < best - 1e-9) {
           best = score;
           out.R = R; out.G = G; out.T = T; out.phasor = ph; out.smem = smem;
@@ -600,6 +602,42 @@ struct DevBuf {
   }
 };
 
+// The device memory pool of the host-buffer entry points (mcmc_cuda and co.):
+// one per device, created by the first call on it, whose freed blocks stay
+// reserved for the next call (release threshold unlimited), so that repeated
+// calls do not map and unmap their device arrays each time.  The pool keeps
+// the largest call's footprint until the process exits.
+inline int host_api_pool(cudaMemPool_t *out)
+{
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static cudaMemPool_t pools[kMaxDev] = {};
+  int dev = 0;
+  CMC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDev) return fail(CMC_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    CMC_CUDA(cudaMemPoolCreate(&p, &props));
+    unsigned long long keep = ~0ull;   // the attribute's value type is a 64-bit unsigned
+    CMC_CUDA(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep));
+    pools[dev] = p;
+  }
+  *out = pools[dev];
+  return CMC_OK;
+}
+
+inline cudaError_t host_api_alloc(void **p, size_t bytes, cudaStream_t s)
+{
+  cudaMemPool_t pool = nullptr;
+  if (host_api_pool(&pool) != CMC_OK) return cudaErrorMemoryAllocation;
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
 inline int read_status(const int *dstatus, cudaStream_t s, int *out)
 {
   CMC_CUDA(cudaMemcpyAsync(out, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -682,7 +720,7 @@ int host_mcmc(float *coor, float *dat, float *std2r, int *icoor, int *idat, floa
   DevBuf buf;
   buf.s = s;
   {
-    cudaError_t e = cudaMallocAsync(&buf.p, a.off, s);
+    cudaError_t e = host_api_alloc(&buf.p, a.off, s);
     if (e != cudaSuccess) {
       buf.p = nullptr;
       return fail(CMC_ERR_NOMEM, std::string("mcmc_cuda: device allocation failed: ") +
@@ -792,7 +830,7 @@ int host_eval(int mode, float *coor, float *dat, float *std2r, int *icoor, int *
   const size_t o_work = a.take(j.work_bytes);
   DevBuf buf;
   buf.s = s;
-  if (cudaMallocAsync(&buf.p, a.off, s) != cudaSuccess) {
+  if (host_api_alloc(&buf.p, a.off, s) != cudaSuccess) {
     buf.p = nullptr;
     return fail(CMC_ERR_NOMEM, "device allocation failed");
   }
