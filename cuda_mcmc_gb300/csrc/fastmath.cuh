@@ -29,16 +29,46 @@ __device__ __forceinline__ void sincospi_poly(float t, float *s, float *c)
   *c = sg * pc;
 }
 
-// sin(pi t), cos(pi t) from the hardware approximations (MUFU.SIN / COS)
-// applied to pi t directly: their absolute error stays below 2^-20.5 for
-// |pi t| <= 100 pi (PTX ISA, sin.approx / cos.approx), and the model's
-// arguments stay within a few pi (|t| = |2 d U| or |Gaussian offset * uv| of
-// a few units), so no explicit range reduction is needed.
+// Single hardware approximations (PTX sin / cos / ex2 / rsqrt .approx.ftz):
+// denormal inputs and results are flushed to zero, which the model's terms
+// never depend on, so no denormal handling is wrapped around them.
+__device__ __forceinline__ float sin_ftz(float x)
+{
+  float y;
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float cos_ftz(float x)
+{
+  float y;
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// 2^x; 2^-inf = 0
+__device__ __forceinline__ float ex2_ftz(float x)
+{
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// 1/sqrt(x) for a positive normal x
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// sin(pi t), cos(pi t) from the hardware approximations applied to pi t
+// directly: their absolute error stays below 2^-20.5 for |pi t| <= 100 pi
+// (PTX ISA, sin.approx / cos.approx), and the model's arguments stay within a
+// few pi (|t| = |2 d U| or |Gaussian offset * uv| of a few units), so no
+// explicit range reduction is needed.
 __device__ __forceinline__ void sincospi_mufu(float t, float *s, float *c)
 {
   const float x = t * 3.14159265358979324f;
-  *s = __sinf(x);
-  *c = __cosf(x);
+  *s = sin_ftz(x);
+  *c = cos_ftz(x);
 }
 
 // sin(x), cos(x) as sin / cos(pi t), t = x / pi, from the polynomials above:
@@ -62,6 +92,19 @@ __device__ __forceinline__ void sincospi_fast(float t, float *s, float *c)
 #endif
 }
 
+// sin(x), cos(x) for the model's arguments (|x| within a few pi, see
+// sincospi_mufu): the hardware approximations, or with CMC_MUFU_SINCOS = 0
+// the polynomials of x / pi.
+__device__ __forceinline__ void sincos_fast(float x, float *s, float *c)
+{
+#if CMC_MUFU_SINCOS
+  *s = sin_ftz(x);
+  *c = cos_ftz(x);
+#else
+  sincospi_poly(x * 0.318309886183790672f, s, c);
+#endif
+}
+
 // atan2(y, x) in [-pi, pi]: a = min/max of |x|, |y| in [0, 1], atan(a) from
 // the polynomial, then the octant.  atan2(0, 0) = 0.
 __device__ __forceinline__ float atan2_poly(float y, float x)
@@ -78,6 +121,42 @@ __device__ __forceinline__ float atan2_poly(float y, float x)
   float r = (ay > ax) ? fmaf(-p, a, 1.57079632679489662f) : p * a;
   if (x < 0.0f) r = 3.14159265358979324f - r;
   return copysignf(r, y);
+}
+
+// F1, F2 as below, at the table coordinate t = kBesselSub |x| - 1/2, which
+// the caller forms with one fmaf.  Interval i = rint(t) and offset
+// d = t - i in [-1/2, 1/2] come from adding 1.5 * 2^23: the float sum is the
+// integer nearest t, held in its low mantissa bits, so that no conversion
+// instructions are needed.  The index is clamped to the table (unsigned min)
+// for any t, NaN and garbage included.  BIG = true: from x = 32 on
+// (t >= kBesselIntervals - 1/2) F1, F2 come from CUDA's j0f / j1f as below.
+template <bool BIG>
+__device__ __forceinline__ void bessel_f12_at(const float4 *tab, float t, float &f1, float &f2)
+{
+  constexpr int kQ = (kBesselDeg + 1) / 2;
+  constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23
+  const float a = __fadd_rn(t, kMagic);
+  const float d = __fsub_rn(t, __fsub_rn(a, kMagic));
+  const unsigned i = min((unsigned)(__float_as_int(a) - __float_as_int(kMagic)),
+                         (unsigned)(kBesselIntervals - 1));
+  const float4 *c = tab + i * kQ;
+  float4 q = c[kQ - 1];
+  float p1 = fmaf(q.z, d, q.x), p2 = fmaf(q.w, d, q.y);
+#pragma unroll
+  for (int m = kQ - 2; m >= 0; --m) {
+    q = c[m];
+    p1 = fmaf(fmaf(p1, d, q.z), d, q.x);
+    p2 = fmaf(fmaf(p2, d, q.w), d, q.y);
+  }
+  f1 = p1;
+  f2 = p2;
+  if (BIG && t >= (float)kBesselIntervals - 0.5f) {
+    const float x = fmaf(t, 1.0f / (float)kBesselSub, 0.5f / (float)kBesselSub);
+    const float ix = 1.0f / x;
+    const float j0 = j0f(x), j1 = j1f(x);
+    f1 = j1 * ix;
+    f2 = fmaf(2.0f, f1, -j0) * ix * ix;
+  }
 }
 
 // F1(x) = J1(x)/x and F2(x) = J2(x)/x^2 (even in x) from the piecewise

@@ -41,6 +41,8 @@
 
 namespace cmc {
 
+// Per-replica constants of the accurate forward pass (the gradient and
+// Fisher kernels, model_sgra_grad.cuh).
 struct SgraConsts {
   float cth, sth;   // rotation by th
   float kex, kin;   // 2 pi Rex, 2 pi Rin (nrad)
@@ -55,34 +57,52 @@ struct SgraConsts {
   int bigx;         // some Bessel argument of this replica is beyond the table
 };
 
+// Per-replica constants of the sampling path (prepare, once per proposal),
+// folded for the fewest operations per model term and held as four float4
+// (four 128-bit shared-memory loads per term):
+//   * Bessel arguments as table coordinates: t = kex8 rho - 1/2 with
+//     kex8 = kBesselSub |2 pi Rex| (F1, F2 are even);
+//   * the ring weight zr folded into the ring coefficients ae, be, ai, bi;
+//   * sin / cos arguments in radians: dsh = 2 pi d, gpu / gpv likewise;
+//   * the Gaussian exponent in base 2 with the axis scales folded into the
+//     rotation: log2 e (gx ug^2 + gy vg^2) = ug'^2 + vg'^2,
+//     ug' = gcx u + gsx v, vg' = gcy v - gsy u;
+//   * a switched-off ring (sgra_model13 Gaussian only) has all of its
+//     coefficients zero, so its terms vanish without a select.
+struct __align__(16) SgraFastConsts {
+  float4 rot;    // cth, sth, kex8, kin8
+  float4 ring;   // zr ae, zr be, zr ai, zr bi: ree = ae F1 - ..., ime = be F2 U - ...
+  float4 gax;    // gcx, gsx, gcy, gsy
+  float4 gph;    // dsh, gpu, gpv, zg: ring shift phase dsh U, Gaussian phase gpu u + gpv v
+  int bigx;      // some Bessel argument of this replica is beyond the table
+  int pad[3];
+};
+
 // Model visibility V = Vre + i Vim of one replica at (u, v), |uv| = rho.
 // Straight-line code: a switched-off component (no inner disk: ai = bi = 0;
-// no Gaussian: zg = 0; sgra_model13 Gaussian-only: ring = 0) contributes
-// zero, so the evaluations of different replicas can be interleaved.
-// Every multiply-add is an explicit fmaf (no a*b + c*d left for the compiler
-// to contract either way), so that the sweep and batch kernels, compiled
-// separately, round identically.
+// no Gaussian: zg = 0; no ring: its coefficients 0) contributes zero, so the
+// evaluations of different replicas can be interleaved.  Every multiply-add
+// is an explicit fmaf (no a*b + c*d left for the compiler to contract either
+// way), so that the sweep and batch kernels, compiled separately, round
+// identically.
 template <bool BIG = true>
-__device__ __forceinline__ float2 sgra_vis(const SgraConsts &c, const float4 *btab, float u,
+__device__ __forceinline__ float2 sgra_vis(const SgraFastConsts &c, const float4 *btab, float u,
                                           float v, float rho)
 {
-  const float U = fmaf(u, c.cth, v * c.sth);
+  const float4 k = c.rot, w = c.ring, g = c.gax, q = c.gph;
+  const float U = fmaf(u, k.x, v * k.y);
   float f1, f2, g1, g2, sd, cd;
-  bessel_f12_tab<BIG>(btab, c.kex * rho, f1, f2);
-  bessel_f12_tab<BIG>(btab, c.kin * rho, g1, g2);
-  sincospi_fast(c.dsh * U, &sd, &cd);
-  const float rei = c.ai * g1, imi = c.bi * g2 * U;
-  const float re = fmaf(c.ae, f1, -fmaf(rei, cd, -(imi * sd)));
-  const float im = fmaf(c.be * f2, U, -fmaf(rei, sd, imi * cd));
-  float vre = c.ring ? c.zr * re : 0.0f;
-  float vim = c.ring ? c.zr * im : 0.0f;
-  const float ug = fmaf(u, c.gc, v * c.gs), vg = fmaf(v, c.gc, -u * c.gs);
-  const float ga = c.zg * __expf(-fmaf(c.gx * ug, ug, c.gy * vg * vg));
+  bessel_f12_at<BIG>(btab, fmaf(k.z, rho, -0.5f), f1, f2);
+  bessel_f12_at<BIG>(btab, fmaf(k.w, rho, -0.5f), g1, g2);
+  sincos_fast(q.x * U, &sd, &cd);
+  const float rei = w.z * g1, imi = w.w * g2 * U;
+  const float re = fmaf(w.x, f1, -fmaf(rei, cd, -(imi * sd)));
+  const float im = fmaf(w.y * f2, U, -fmaf(rei, sd, imi * cd));
+  const float ug = fmaf(u, g.x, v * g.y), vg = fmaf(v, g.z, -(u * g.w));
+  const float ga = q.w * ex2_ftz(-fmaf(ug, ug, vg * vg));
   float sg, cg;
-  sincospi_fast(fmaf(c.gpu, u, c.gpv * v), &sg, &cg);
-  vre = fmaf(ga, cg, vre);
-  vim = fmaf(ga, sg, vim);
-  return make_float2(vre, vim);
+  sincos_fast(fmaf(q.y, u, q.z * v), &sg, &cg);
+  return make_float2(fmaf(ga, cg, re), fmaf(ga, sg, im));
 }
 
 // Data packing kernels (defined once, in the library translation unit).
@@ -96,14 +116,14 @@ __global__ void sgra_scatter_kernel(const float4 *raw, const float *key, const i
                                     int cpext, float4 *vis, float *rho, int *orig, int4 *cli,
                                     float4 *clf, int *aux, int *status);
 
-// CMC_BRANCHFREE: evaluate every local replica and drop the terms of the
-// inactive ones, so that the R independent evaluations interleave.
+// CMC_BRANCHFREE: evaluate every local replica, inactive ones included (their
+// sums are discarded), so that the R independent evaluations interleave.
 #ifndef CMC_BRANCHFREE
 #define CMC_BRANCHFREE 1
 #endif
 
 struct SgraModel {
-  using Consts = SgraConsts;
+  using Consts = SgraFastConsts;
   struct Packed {
     const float4 *vis;   // [npts] sorted by |uv|: u, v, amp_obs, 1/sigma^2 (0: triangle point)
     const float *rho;    // [npts] |uv| of vis
@@ -235,7 +255,7 @@ struct SgraModel {
   template <class Cta>
   __device__ static void prepare(Cta &cta, int r, const float *p)
   {
-    SgraConsts &c = cta.consts[r];
+    SgraFastConsts &c = cta.consts[r];
     const float pi = 3.1415926535897931f;
     const int im = cta.pk->imodel;
     const float Zsp = p[0], Re = p[1], rq = p[2], ecc = p[3], fade = p[4];
@@ -263,50 +283,60 @@ struct SgraModel {
                                        fmaf(-(Rin * Rin), 1.0f - dr, Rex * Rex));
     const float h0 = __fmul_rn(fade, h);
     const float hm = (h - h0) * (-0.25f / pi);      // -(h - h0) / (4 pi)
-    sincos_fma(th, &c.sth, &c.cth);
-    c.kex = 2.0f * pi * Rex;
-    c.kin = 2.0f * pi * Rin;
-    c.ae = 0.5f * (h + h0) * Rex * c.kex;
-    c.be = hm * (c.kex * c.kex * c.kex);
-    c.inner = (Rin != 0.0f);
-    c.ai = c.inner ? 0.5f * fmaf(-dr, h - h0, h + h0) * Rin * c.kin : 0.0f;
-    c.bi = c.inner ? hm * rq * (c.kin * c.kin * c.kin) : 0.0f;
-    c.dsh = 2.0f * d;
-    // 2 (pi / (2 sqrt(2 ln 2)))^2 = pi^2 / (4 ln 2): FWHM^2 -> Gaussian exponent
-    const float gcoef = 3.5597039f;
-    const float gsy = gax * Rex, gsx = aq * gsy;
-    c.gx = gcoef * gsx * gsx;
-    c.gy = gcoef * gsy * gsy;
-    c.gauss = !(gax == 0.0f || aq == 0.0f || gq == 0.0f);
+    float sth, cth;
+    sincos_fma(th, &sth, &cth);
+    const float kex = 2.0f * pi * Rex;
+    const float kin = 2.0f * pi * Rin;
+    const bool inner = (Rin != 0.0f);
+    float ae = 0.5f * (h + h0) * Rex * kex;
+    float be = hm * (kex * kex * kex);
+    float ai = inner ? 0.5f * fmaf(-dr, h - h0, h + h0) * Rin * kin : 0.0f;
+    float bi = inner ? hm * rq * (kin * kin * kin) : 0.0f;
+    float dsh = 2.0f * d;
+    float kex8 = fabsf(kex) * (float)kBesselSub, kin8 = fabsf(kin) * (float)kBesselSub;
+    // Gaussian: exponent (pi / (2 sqrt(2 ln 2)))^2 2 (FWHM projections)^2,
+    // i.e. pi^2 / (4 ln 2) (gsx^2 ug^2 + gsy^2 vg^2); in base 2 the axis
+    // scales are K gsx and K gsy with K = sqrt(log2 e pi^2 / (4 ln 2)) =
+    // pi / (2 ln 2)
+    const float K = 2.2661800709135966f;
+    const float sy = K * (gax * Rex), sx = aq * sy;
+    float gc, gs, gpu, gpv;
+    bool gauss = !(gax == 0.0f || aq == 0.0f || gq == 0.0f);
     if (im == 1) {
       const float gshift = Rin - d;
-      c.gc = c.cth;
-      c.gs = c.sth;
-      c.gpu = -2.0f * gshift * c.cth;
-      c.gpv = -2.0f * gshift * c.sth;
+      gc = cth;
+      gs = sth;
+      gpu = -2.0f * gshift * cth;
+      gpv = -2.0f * gshift * sth;
     } else {
       float sa, ca;
-      sincos_fma(beta, &c.gs, &c.gc);
+      sincos_fma(beta, &gs, &gc);
       sincos_fma(alpha, &sa, &ca);
-      c.gpu = -2.0f * gr * Rex * ca;
-      c.gpv = -2.0f * gr * Rex * sa;
+      gpu = -2.0f * gr * Rex * ca;
+      gpv = -2.0f * gr * Rex * sa;
     }
-    if (c.gauss) {
-      c.zr = Zsp * (1.0f - gq);
-      c.zg = Zsp * gq;
-    } else {
-      c.zr = Zsp;
-      c.zg = 0.0f;
+    float zr = Zsp, zg = 0.0f;
+    if (gauss) {
+      zr = Zsp * (1.0f - gq);
+      zg = Zsp * gq;
     }
-    c.ring = 1;
     if (im != 1 && gq == 1.0f) {   // sgra_model13: Gaussian only (model.cuh:204-210)
-      c.ring = 0;
-      c.zg = Zsp;
-      c.gauss = !(gax == 0.0f || aq == 0.0f);
+      zr = 0.0f;
+      ae = be = ai = bi = dsh = kex8 = kin8 = 0.0f;
+      zg = Zsp;
+      gauss = !(gax == 0.0f || aq == 0.0f);
     }
-    if (!c.gauss) c.zg = 0.0f;
+    if (!gauss) zg = 0.0f;
+    c.rot = make_float4(cth, sth, kex8, kin8);
+    c.ring = make_float4(zr * ae, zr * be, zr * ai, zr * bi);
+    c.gax = make_float4(gc * sx, gs * sx, gc * sy, gs * sy);
+    c.gph = make_float4(pi * dsh, pi * gpu, pi * gpv, zg);
+    // the straight-line loops may use the table while every coordinate
+    // t = kex8 rho - 1/2 of the data stays below kBesselIntervals - 3/2 (one
+    // interval of margin for the rounding of the products)
     const float rho_max = (cta.pk->npts > 0) ? __int_as_float(__ldg(&cta.pk->aux[1])) : 0.0f;
-    c.bigx = !(fmaxf(fabsf(c.kex), fabsf(c.kin)) * rho_max < (float)kBesselXmax);
+    c.bigx = !(fmaxf(kex8, kin8) * rho_max < (float)(kBesselIntervals - 1));
+    c.pad[0] = c.pad[1] = c.pad[2] = 0;
   }
 
   // chi^2 of every active replica over all data (both passes).  The phase
@@ -339,12 +369,15 @@ struct SgraModel {
     const float4 *btab = reinterpret_cast<const float4 *>(cta.scratch);
     float *zs = GL ? pk.gph + (size_t)cta.ph_region * npts : cta.scratch + kTabBytes / 4;
     float2 *z = reinterpret_cast<float2 *>(zs);
+#if !CMC_BRANCHFREE
     bool act[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      acc[r] = 0.0f;
-      act[r] = cta.flag[r] != 0;
-    }
+    for (int r = 0; r < R; ++r) act[r] = cta.flag[r] != 0;
+#endif
+    // Every local replica is evaluated (branch-free); the sums of the
+    // inactive ones (flag 0) are never read, so their terms need no mask.
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = 0.0f;
     // One model term per (point, replica); the points are packed closure
     // corners first, so only the first nused need a phase: each thread walks
     // its stride through [0, nused) with phases, then on without.
@@ -358,15 +391,18 @@ struct SgraModel {
 #endif
         const float2 V = sgra_vis<BIG>(cta.consts[r], btab, d.x, d.y, rho);
         const float n2 = fmaf(V.x, V.x, V.y * V.y);
-        const float rs = (n2 > 0.0f) ? rsqrtf(n2) : 0.0f;
-        const float dif = fmaf(-n2, rs, d.z);
-        acc[r] = fmaf(act[r] ? dif * dif : 0.0f, d.w, acc[r]);
-        if constexpr (decltype(with_phase)::value) {
-          if (PH)
+        if (PH) {
+          const float rs = (n2 > 0.0f) ? rsqrt_ftz(n2) : 0.0f;
+          const float dif = fmaf(-n2, rs, d.z);
+          acc[r] = fmaf(dif * dif, d.w, acc[r]);
+          if constexpr (decltype(with_phase)::value)
             z[r * npts + i] = (n2 > 0.0f) ? make_float2(V.x * rs, V.y * rs)
                                           : make_float2(1.f, 0.f);
-          else
-            zs[r * npts + i] = atan2_poly(V.y, V.x);
+        } else {
+          // |V| = n2 / sqrt(n2), n2 held off zero (and denormals): |V| -> 0
+          const float dif = fmaf(-n2, rsqrt_ftz(fmaxf(n2, 1e-30f)), d.z);
+          acc[r] = fmaf(dif * dif, d.w, acc[r]);
+          if constexpr (decltype(with_phase)::value) zs[r * npts + i] = atan2_poly(V.y, V.x);
         }
       }
     };
@@ -396,7 +432,7 @@ struct SgraModel {
           const float x = f.w - (zs[r * npts + q.x] + zs[r * npts + q.y] - zs[r * npts + q.z]);
           dif = fmaf(-6.2831853071795865f, rintf(x * 0.15915494309189535f), x);
         }
-        acc[r] = fmaf(act[r] ? dif * dif : 0.0f, f.z, acc[r]);
+        acc[r] = fmaf(dif * dif, f.z, acc[r]);
       }
     }
   }
