@@ -111,6 +111,27 @@ def evals_per_step(w, args):
     return (args.burn_per_step + args.main_per_step) * w.nprm * w.nbeta * w.nseq
 
 
+# DRAM bytes of one sweep launch of the 2000 vis + 600 closure, 64 x 32 workload:
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of a 16-iteration launch
+# (4 burn-in + 12 recorded; 29.5 + 33.4 MB) = a fixed part (state, model data per
+# CTA, final datm / chi2m rows) plus the records of each main iteration (pout +
+# tout + chi2, 9*32*64*4 + 32*64*4 + 64*4 bytes).
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 16-iteration launch "
+                  "(62.9 MB) scaled to this launch: fixed part + the records of each main "
+                  "iteration; only for the 2000 vis + 600 closure 64 x 32 workload")
+_TRAFFIC_CAPTURE = 62.9e6
+_TRAFFIC_REC_PER_ITER = 9 * 32 * 64 * 4 + 32 * 64 * 4 + 64 * 4
+
+
+def sweep_traffic(w, args):
+    """DRAM bytes per sweep launch (the timed step is one launch), or None when
+    the workload is not the profiled one."""
+    if (w.nvis, w.ndat - w.nvis, w.nseq, w.nbeta) != (2000, 600, 64, 32):
+        return None
+    fixed = _TRAFFIC_CAPTURE - 12 * _TRAFFIC_REC_PER_ITER
+    return fixed + args.main_per_step * _TRAFFIC_REC_PER_ITER
+
+
 def flop_per_eval(w):
     return w.nvis * FLOP_PER_AMP + (w.ndat - w.nvis) * FLOP_PER_CPH
 
@@ -394,7 +415,8 @@ def run_mine(args, rank, world, local):
             "l2": "2x L2 buffer written between timed steps",
             "launch": cfg},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": sweep_traffic(w, args),
+                     "traffic_source": TRAFFIC_SOURCE,
                      "peak_source": "measured cuBLAS SGEMM (TF32 off) in this run",
                      "flop_per_eval": flop_per_eval(w)},
         "clocks": clocks,

@@ -25,6 +25,7 @@
 // seed it walks the same chains (cuRAND XORWOW, curand_init(seed, ist, 0)).
 #pragma once
 #include <cooperative_groups.h>
+#include <cstring>
 #include <cuda_runtime.h>
 #include <curand_kernel.h>
 
@@ -39,11 +40,18 @@ constexpr int kRepF = 4;         // per-replica floats: ptent, chi2c, chi2n, bet
 constexpr int kRepI = 4;         // per-replica ints: ptentn, flag, kchosen, evaluated
 constexpr int kMaxRetry = 64;    // bound on the k-redraw loops (u == 1.0 exactly)
 
-// Angle wrapped into [-pi, pi] as the reference does (atan2(sin, cos),
-// src/gpu_mcmc.cu:389-393).  Out of line: one compiled body shared by every
-// kernel and call site of a translation unit, so that the sweep and batch
-// kernels round it identically whatever the compiler does around the call.
-static __device__ __noinline__ float wrap_pi(float p) { return atan2f(sinf(p), cosf(p)); }
+// Angle wrapped into [-pi, pi], the value of the reference's atan2(sin p,
+// cos p) (src/gpu_mcmc.cu:389-393): p - 2 pi n with n = rint(p / (2 pi)),
+// in double precision and rounded once to float, i.e. the float nearest the
+// exact wrap (the reference's float sin / cos / atan2 come within an ulp or
+// two of it).  A short fixed sequence (multiply, rint, fma, conversion) with
+// nothing left to contraction, so every kernel rounds it identically.
+__device__ __forceinline__ float wrap_pi(float p)
+{
+  const double x = (double)p;
+  const double n = rint(x * 0.15915494309189533577);
+  return (float)fma(-6.283185307179586477, n, x);
+}
 
 __device__ __forceinline__ void set_status(int *st, int code)
 {
@@ -97,6 +105,22 @@ struct Rng {
   }
 };
 
+// Copy of lane `src`'s value of a trivially copyable object on every lane of
+// the (fully active) warp, word by word.
+template <class V>
+__device__ __forceinline__ V warp_broadcast(const V &v, int src)
+{
+  static_assert(sizeof(V) % 4 == 0, "warp_broadcast: size must be a multiple of 4 bytes");
+  constexpr int kW = (int)(sizeof(V) / 4);
+  int w[kW];
+  memcpy(w, &v, sizeof(V));
+#pragma unroll
+  for (int i = 0; i < kW; ++i) w[i] = __shfl_sync(0xffffffffu, w[i], src);
+  V out;
+  memcpy(&out, w, sizeof(V));
+  return out;
+}
+
 __host__ __device__ inline unsigned align16(unsigned x) { return (x + 15u) & ~15u; }
 
 // Shared-memory plan of one CTA; the same function sizes the launch on the
@@ -146,6 +170,8 @@ struct Cta {
   int tid, nthreads;
   int ph_region;                    // first of R consecutive per-replica regions of a
                                     // global model scratch (disjoint between CTAs)
+  int model_i;                      // one int and one float a model may cache at
+  float model_f;                    // setup (read once per launch, held in registers)
 };
 
 template <class Model, int R>

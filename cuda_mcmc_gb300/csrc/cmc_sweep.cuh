@@ -306,27 +306,73 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
     if (tid < R) accept_adjust(tid, burn);
 
     // ---- replica_exchange (src/gpu_mcmc.cu:533-626) ------------------------
+    // nbeta attempts in the reference's order, drawn from the ibeta = 0
+    // replica's generator (thread 0 of cluster rank 0).
     cluster.sync();
-    if (rank == 0) {
-      // gather the nbeta chi^2 values in parallel (one remote load each)
-      for (int s = tid; s < nbeta; s += T) {
-        x_chi2[s] = cluster.map_shared_rank(s_chi2c, s / R)[s % R];
-        x_perm[s] = s;
+    if (nbeta <= 32) {
+      // Warp 0 of rank 0, slot s on lane s: chi^2, tcur, owner and n_exch in
+      // registers, swaps by shuffles.  Every lane runs a copy of thread 0's
+      // generator (the same draws), so k and u are known warp-wide and the
+      // attempt loop has no shared-memory round trips; lane 0 keeps the
+      // advanced generator.
+      if (rank == 0 && tid < 32) {
+        const int lane = tid;
+        const bool slot = lane < nbeta;
+        float chi = slot ? cluster.map_shared_rank(s_chi2c, lane / R)[lane % R] : 0.0f;
+        const float bt = slot ? x_beta[lane] : 0.0f;
+        int tc = slot ? x_tcur[lane] : 0, own = lane, nx = slot ? x_nexch[lane] : 0;
+        Rng xr = warp_broadcast(rng, 0);
+        const int nb1 = nbeta - 1;
+        for (int ib = 0; ib < nbeta; ++ib) {
+          const int k = xr.index(nb1, job.status);
+          const float ck = __shfl_sync(0xffffffffu, chi, k);
+          const float ck1 = __shfl_sync(0xffffffffu, chi, k + 1);
+          const float bk = __shfl_sync(0xffffffffu, bt, k);
+          const float bk1 = __shfl_sync(0xffffffffu, bt, k + 1);
+          const int tk = __shfl_sync(0xffffffffu, tc, k), tk1 = __shfl_sync(0xffffffffu, tc, k + 1);
+          const int ok = __shfl_sync(0xffffffffu, own, k), ok1 = __shfl_sync(0xffffffffu, own, k + 1);
+          const float a = expf(-0.5f * (bk1 - bk) * (ck - ck1));
+          const float alpha = (a < 1.0f) ? a : 1.0f;
+          const float u = xr.uniform();
+          if (u <= alpha) {
+            if (lane == k) {
+              chi = ck1; tc = tk1; own = ok1;
+              if (!burn) nx += 1;
+            } else if (lane == k + 1) {
+              chi = ck; tc = tk; own = ok;
+            }
+          }
+        }
+        if (lane == 0) rng = xr;
+        if (slot) {
+          x_chi2[lane] = chi;
+          x_tcur[lane] = tc;
+          x_perm[lane] = own;
+          x_nexch[lane] = nx;
+        }
       }
-      __syncthreads();
-    }
-    if (rank == 0 && tid == 0) {
-      const int nb1 = nbeta - 1;
-      for (int ib = 0; ib < nbeta; ++ib) {
-        const int k = rng.index(nb1, job.status);
-        const float a = expf(-0.5f * (x_beta[k + 1] - x_beta[k]) * (x_chi2[k] - x_chi2[k + 1]));
-        const float alpha = (a < 1.0f) ? a : 1.0f;
-        const float u = rng.uniform();
-        if (u <= alpha) {
-          int ti = x_tcur[k]; x_tcur[k] = x_tcur[k + 1]; x_tcur[k + 1] = ti;
-          int pi = x_perm[k]; x_perm[k] = x_perm[k + 1]; x_perm[k + 1] = pi;
-          float cc = x_chi2[k]; x_chi2[k] = x_chi2[k + 1]; x_chi2[k + 1] = cc;
-          if (!burn) x_nexch[k] += 1;
+    } else {
+      if (rank == 0) {
+        // gather the nbeta chi^2 values in parallel (one remote load each)
+        for (int s = tid; s < nbeta; s += T) {
+          x_chi2[s] = cluster.map_shared_rank(s_chi2c, s / R)[s % R];
+          x_perm[s] = s;
+        }
+        __syncthreads();
+      }
+      if (rank == 0 && tid == 0) {
+        const int nb1 = nbeta - 1;
+        for (int ib = 0; ib < nbeta; ++ib) {
+          const int k = rng.index(nb1, job.status);
+          const float a = expf(-0.5f * (x_beta[k + 1] - x_beta[k]) * (x_chi2[k] - x_chi2[k + 1]));
+          const float alpha = (a < 1.0f) ? a : 1.0f;
+          const float u = rng.uniform();
+          if (u <= alpha) {
+            int ti = x_tcur[k]; x_tcur[k] = x_tcur[k + 1]; x_tcur[k + 1] = ti;
+            int pi = x_perm[k]; x_perm[k] = x_perm[k + 1]; x_perm[k + 1] = pi;
+            float cc = x_chi2[k]; x_chi2[k] = x_chi2[k + 1]; x_chi2[k + 1] = cc;
+            if (!burn) x_nexch[k] += 1;
+          }
         }
       }
     }

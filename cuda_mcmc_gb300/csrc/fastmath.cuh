@@ -113,9 +113,10 @@ __device__ __forceinline__ float atan2_poly(float y, float x)
   const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
   const float a = (mx > 0.0f) ? __fdividef(mn, mx) : 0.0f;
   const float s = a * a;
-  float p = kAtanP[9];
+  constexpr int kN = (int)(sizeof(kAtanP) / sizeof(kAtanP[0]));
+  float p = kAtanP[kN - 1];
 #pragma unroll
-  for (int k = 8; k >= 0; --k) p = fmaf(p, s, kAtanP[k]);
+  for (int k = kN - 2; k >= 0; --k) p = fmaf(p, s, kAtanP[k]);
   // pi/2 - p a as an explicit fmaf: no multiply-add is left for the compiler
   // to contract differently in different kernels
   float r = (ay > ax) ? fmaf(-p, a, 1.57079632679489662f) : p * a;

@@ -62,7 +62,7 @@ def cospi(s):
 
 
 def main():
-    at = fit(atan_over_a, 0.0, 1.0, 9)
+    at = fit(atan_over_a, 0.0, 1.0, 7)
     sn = fit(sinpi_over_r, 0.0, 0.25, 5)
     cs = fit(cospi, 0.0, 0.25, 6)
     a = np.linspace(0, 1, 200001)

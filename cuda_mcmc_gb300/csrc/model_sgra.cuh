@@ -242,6 +242,10 @@ struct SgraModel {
   template <class Cta>
   __device__ static void setup(Cta &cta, int tid, int T)
   {
+    // cached: model_i = nused (points that need a phase), model_f = max |uv|
+    const Packed &pk = *cta.pk;
+    cta.model_i = (pk.ncph > 0 && pk.npass >= 2) ? __ldg(&pk.aux[0]) : 0;
+    cta.model_f = (pk.npts > 0) ? __int_as_float(__ldg(&pk.aux[1])) : 0.0f;
     float4 *tab = reinterpret_cast<float4 *>(cta.scratch);
     const float4 *src = &kBesselTab[0][0];
     for (int i = tid; i < (int)(kTabBytes / sizeof(float4)); i += T) tab[i] = src[i];
@@ -334,8 +338,7 @@ struct SgraModel {
     // the straight-line loops may use the table while every coordinate
     // t = kex8 rho - 1/2 of the data stays below kBesselIntervals - 3/2 (one
     // interval of margin for the rounding of the products)
-    const float rho_max = (cta.pk->npts > 0) ? __int_as_float(__ldg(&cta.pk->aux[1])) : 0.0f;
-    c.bigx = !(fmaxf(kex8, kin8) * rho_max < (float)(kBesselIntervals - 1));
+    c.bigx = !(fmaxf(kex8, kin8) * cta.model_f < (float)(kBesselIntervals - 1));
     c.pad[0] = c.pad[1] = c.pad[2] = 0;
   }
 
@@ -406,7 +409,7 @@ struct SgraModel {
         }
       }
     };
-    const int nused = (pk.ncph > 0 && pk.npass >= 2) ? __ldg(&pk.aux[0]) : 0;
+    const int nused = cta.model_i;
     int i = tid;
     for (; i < nused; i += T) terms(i, std::true_type{});
     for (; i < npts; i += T) terms(i, std::false_type{});
