@@ -112,6 +112,10 @@ inline bool global_phases_ok(const typename Model::Packed &pk)
   else return false;
 }
 
+// Data terms per replica evaluation up to which a sweep is latency-bound (the
+// launch-shape ranking below then minimises the work per CTA).
+constexpr int kFewPoints = 64;
+
 // Pick replicas-per-CTA R (cluster size G = nbeta/R <= 16), threads T and the
 // phase storage mode by the ranking below (autotune.py measures instead).
 template <class Model>
@@ -147,16 +151,25 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         });
         if (n <= 0) continue;
         const int waves = (j.nseq + n - 1) / n;
-        // Measured on GB300 (Sgr A*, 2000-20000 visibilities): fewest waves
-        // of resident clusters first; then about 32 threads per replica
-        // (16 or 64 cost ~10 %); then the phase storage (phasors, phases in
-        // shared memory, phases in global memory: an L2 round trip per
-        // closure gather); then more replicas per CTA (more independent
-        // work per thread).  Lexicographic, lower is better.
-        const int tpr = T / R;
-        const int shape_rank = (tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2;
-        const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
-        const double score = waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 - R;
+        // Measured on GB300, lexicographic, lower is better.  Fewest waves of
+        // resident clusters first.  Then, with a few data terms per replica
+        // (the plugin models: ndat 1-8), the per-proposal serial work of a
+        // CTA's R replicas is the time: fewest replicas per CTA, then fewest
+        // threads (Rosenbrock, 16 x 32: R=2 T=64 4.3 ms, R=8 T=256 6.9 ms).
+        // Otherwise (Sgr A*, 2000-20000 visibilities) about 32 threads per
+        // replica (16 or 64 cost ~10 %); then the phase storage (phasors,
+        // phases in shared memory, phases in global memory: an L2 round trip
+        // per closure gather); then more replicas per CTA (more independent
+        // work per thread).
+        double score;
+        if (Model::points(q) <= kFewPoints) {
+          score = waves * 1000.0 + R * 10.0 + T / 64;
+        } else {
+          const int tpr = T / R;
+          const int shape_rank = (tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2;
+          const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
+          score = waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 - R;
+        }
         if (score < best - 1e-9) {
           best = score;
           out.R = R; out.G = G; out.T = T; out.phasor = ph; out.smem = smem;
