@@ -128,9 +128,11 @@ __device__ __forceinline__ float atan2_poly(float y, float x)
 // the caller forms with one fmaf.  Interval i = rint(t) and offset
 // d = t - i in [-1/2, 1/2] come from adding 1.5 * 2^23: the float sum is the
 // integer nearest t, held in its low mantissa bits, so that no conversion
-// instructions are needed.  The index is clamped to the table (unsigned min)
-// for any t, NaN and garbage included.  BIG = true: from x = 32 on
-// (t >= kBesselIntervals - 1/2) F1, F2 come from CUDA's j0f / j1f as below.
+// instructions are needed.  BIG = false: the caller guarantees
+// -1/2 <= t < kBesselIntervals - 1/2 (no index check).  BIG = true: any t,
+// NaN and garbage included; the index is clamped to the table (unsigned
+// min), and from x = 32 on (t >= kBesselIntervals - 1/2) F1, F2 come from
+// CUDA's j0f / j1f as below.
 template <bool BIG>
 __device__ __forceinline__ void bessel_f12_at(const float4 *tab, float t, float &f1, float &f2)
 {
@@ -138,8 +140,8 @@ __device__ __forceinline__ void bessel_f12_at(const float4 *tab, float t, float 
   constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23
   const float a = __fadd_rn(t, kMagic);
   const float d = __fsub_rn(t, __fsub_rn(a, kMagic));
-  const unsigned i = min((unsigned)(__float_as_int(a) - __float_as_int(kMagic)),
-                         (unsigned)(kBesselIntervals - 1));
+  unsigned i = (unsigned)(__float_as_int(a) - __float_as_int(kMagic));
+  if (BIG) i = min(i, (unsigned)(kBesselIntervals - 1));
   const float4 *c = tab + i * kQ;
   float4 q = c[kQ - 1];
   float p1 = fmaf(q.z, d, q.x), p2 = fmaf(q.w, d, q.y);

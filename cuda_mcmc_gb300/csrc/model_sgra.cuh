@@ -239,11 +239,17 @@ struct SgraModel {
 
   static int host_pack(const cmc_job &j, Packed &pk, void *work, cudaStream_t s);
 
+  // Bessel table into shared memory; every local replica's constants zeroed
+  // (a valid in-table state for replicas not yet prepared).
   template <class Cta>
   __device__ static void setup(Cta &cta, int tid, int T)
   {
     // cached: model_i = nused (points that need a phase), model_f = max |uv|
     const Packed &pk = *cta.pk;
+    constexpr int kWords =
+        (int)(sizeof(SgraFastConsts) / 4) * (int)std::extent<decltype(Cta::ist)>::value;
+    int *cz = reinterpret_cast<int *>(cta.consts);
+    for (int i = tid; i < kWords; i += T) cz[i] = 0;
     cta.model_i = (pk.ncph > 0 && pk.npass >= 2) ? __ldg(&pk.aux[0]) : 0;
     cta.model_f = (pk.npts > 0) ? __int_as_float(__ldg(&pk.aux[1])) : 0.0f;
     float4 *tab = reinterpret_cast<float4 *>(cta.scratch);
@@ -344,13 +350,16 @@ struct SgraModel {
 
   // chi^2 of every active replica over all data (both passes).  The phase
   // storage mode and the need for the out-of-table Bessel path are uniform
-  // over the CTA: each combination is its own straight-line loop.
+  // over the CTA: each combination is its own straight-line loop.  The
+  // table-only loop runs when no local replica, active or not (the inactive
+  // ones are evaluated too, with their last or zeroed constants), reaches
+  // beyond the table: its lookups need no index check.
   template <int R, class Cta>
   __device__ static void eval(Cta &cta, float (&acc)[R])
   {
     bool big = false;
 #pragma unroll
-    for (int r = 0; r < R; ++r) big |= (cta.flag[r] != 0 && cta.consts[r].bigx != 0);
+    for (int r = 0; r < R; ++r) big |= (cta.consts[r].bigx != 0);
     if (cta.pk->phasor == 1) {
       if (big) eval_impl<R, true, true, false>(cta, acc);
       else eval_impl<R, true, false, false>(cta, acc);
