@@ -171,16 +171,21 @@ def _sgra_cpext(w, seed=12):
         icoor=np.zeros(1, np.int32), idat=np.array([nvis, 0, 1], np.int32))
 
 
-@pytest.mark.parametrize("cfg", ["sgra", "sgra_cpext", "sgra_npass1", "nlsys", "rosenbrock"])
+@pytest.mark.parametrize("cfg", ["sgra", "sgra_cpext", "sgra_npass1", "sgra_nbeta64", "nlsys",
+                                 "rosenbrock"])
 def test_sweep_lockstep_vs_fp64_oracle(cfg):
     """Larger data than the fixtures: from the same state and the same
     injected draws, every iteration of the kernel makes the FP64 oracle's
     decisions (near ties excepted) and reaches its chi^2 within 1e-5.
     Sgr A* with closures from visibility triplets, from triangle corners
-    (cpExt = 1) and without the closure pass (npass = 1)."""
+    (cpExt = 1), without the closure pass (npass = 1), and with 64
+    temperatures (the exchange's shared-memory loop; up to 32 it runs on the
+    lanes of one warp)."""
     import dataclasses
     if cfg == "sgra":
         w = synth.sgra(nvis=400, ncph=120, seed=8, nseq=2, nbeta=8)
+    elif cfg == "sgra_nbeta64":
+        w = synth.sgra(nvis=200, ncph=60, seed=8, nseq=1, nbeta=64)
     elif cfg == "sgra_cpext":
         w = _sgra_cpext(synth.sgra(nvis=400, ncph=120, seed=8, nseq=2, nbeta=8))
     elif cfg == "sgra_npass1":
