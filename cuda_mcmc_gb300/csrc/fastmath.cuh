@@ -59,18 +59,6 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
   return y;
 }
 
-// sin(pi t), cos(pi t) from the hardware approximations applied to pi t
-// directly: their absolute error stays below 2^-20.5 for |pi t| <= 100 pi
-// (PTX ISA, sin.approx / cos.approx), and the model's arguments stay within a
-// few pi (|t| = |2 d U| or |Gaussian offset * uv| of a few units), so no
-// explicit range reduction is needed.
-__device__ __forceinline__ void sincospi_mufu(float t, float *s, float *c)
-{
-  const float x = t * 3.14159265358979324f;
-  *s = sin_ftz(x);
-  *c = cos_ftz(x);
-}
-
 // sin(x), cos(x) as sin / cos(pi t), t = x / pi, from the polynomials above:
 // rint, multiplies and explicit fmaf only, so that every kernel and call site
 // rounds it identically (the per-proposal constants of the sweep and batch
@@ -83,18 +71,13 @@ __device__ __forceinline__ void sincos_fma(float x, float *s, float *c)
 #ifndef CMC_MUFU_SINCOS
 #define CMC_MUFU_SINCOS 1
 #endif
-__device__ __forceinline__ void sincospi_fast(float t, float *s, float *c)
-{
-#if CMC_MUFU_SINCOS
-  sincospi_mufu(t, s, c);
-#else
-  sincospi_poly(t, s, c);
-#endif
-}
 
-// sin(x), cos(x) for the model's arguments (|x| within a few pi, see
-// sincospi_mufu): the hardware approximations, or with CMC_MUFU_SINCOS = 0
-// the polynomials of x / pi.
+// sin(x), cos(x) for the model's arguments: the hardware approximations
+// applied to x directly -- their absolute error stays below 2^-20.5 for
+// |x| <= 100 pi (PTX ISA, sin.approx / cos.approx), and the arguments stay
+// within a few pi (the ring shift 2 pi d U and the Gaussian offset phase, of
+// a few units), so no explicit range reduction is needed.  With
+// CMC_MUFU_SINCOS = 0, the polynomials of x / pi.
 __device__ __forceinline__ void sincos_fast(float x, float *s, float *c)
 {
 #if CMC_MUFU_SINCOS
