@@ -160,7 +160,9 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         // replica (16 or 64 cost ~10 %); then the phase storage (phasors,
         // phases in shared memory, phases in global memory: an L2 round trip
         // per closure gather); then more replicas per CTA (more independent
-        // work per thread).
+        // work per thread), except with phases in global memory, where 4
+        // replicas per CTA do best (20000 visibilities: R=4 T=128 11.1 ms,
+        // R=8 T=256 12.7 ms per 4 iterations).
         double score;
         if (Model::points(q) <= kFewPoints) {
           score = waves * 1000.0 + R * 10.0 + T / 64;
@@ -168,7 +170,8 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
           const int tpr = T / R;
           const int shape_rank = (tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2;
           const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
-          score = waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 - R;
+          const double r_rank = (ph == 2) ? (double)std::abs(R - 4) : -(double)R;
+          score = waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 + r_rank;
         }
         if (score < best - 1e-9) {
           best = score;
