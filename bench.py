@@ -420,7 +420,9 @@ def run_mine(args, rank, world, local):
                      "peak_source": "measured cuBLAS SGEMM (TF32 off) in this run",
                      "flop_per_eval": flop_per_eval(w)},
         "clocks": clocks,
-        "gpu_launches": 2 * args.steps,
+        # per step (one cmc_run): the packing kernels (points, closure-corner
+        # marks when there are closures, rank, scatter) and the sweep kernel
+        "gpu_launches": args.steps * (4 + (1 if w.ndat > w.nvis else 0)),
     }
     if not args.no_e2e and world == 1:
         e2e, e2e_step, h2d, d2h = e2e_rate(w, args, steps=args.steps, warmup=1)
