@@ -431,10 +431,30 @@ def get_time_indices(tsec):
     return ibeg, iend
 
 
+_TRIANGLES = {}
+
+
+def _triangle_slots(na):
+    """All index triplets i < j < k of range(na), in itertools.combinations
+    order, as an [ntri, 3] array (cached per na)."""
+    t = _TRIANGLES.get(na)
+    if t is None:
+        t = np.array(list(itertools.combinations(range(na), 3)), np.int64).reshape(-1, 3)
+        _TRIANGLES[na] = t
+    return t
+
+
 def calc_closures(phase, tsec, blin):
     """Closure phases phi(a1a2) + phi(a1a3) - phi(a2a3) of every antenna
     triangle of every equal-time span: returns cphs, cpix (row triplets),
-    trid (triangle ids) and tcphsec (times)."""
+    trid (triangle ids) and tcphsec (times).
+
+    The reference's loop (src/imgpu.py:1229-1325), vectorised per span: the
+    span's antennas sorted (np.unique), the first row of every baseline a-b
+    in a [na, na] table, all triangles of the span at once in
+    itertools.combinations order.  As in the reference, every triangle of a
+    span's antennas must have its three baselines in the span (IndexError
+    otherwise)."""
     empty = (np.array([], np.float32), np.zeros((0, 3), np.int32), np.array([], np.int32),
              np.array([], np.float32))
     if len(phase) < 3:
@@ -442,22 +462,38 @@ def calc_closures(phase, tsec, blin):
     ibeg, iend = get_time_indices(tsec)
     if not ibeg:
         return empty
-    cphs, cpix, trid, tcp = [], [], [], []
+    phase = np.asarray(phase)
     bls = np.asarray(blin)
+    cphs, cpix, trid, tcp = [], [], [], []
     for i0, i1 in zip(ibeg, iend):
-        bl = bls[i0:i1].astype(int)
+        bl = bls[i0:i1].astype(np.int64)
         ant = np.unique(bl)
-        for a1, a2, a3 in (ant[list(t)] for t in itertools.combinations(range(ant.size), 3)):
-            ib1 = i0 + int(np.where((bl[:, 0] == a1) & (bl[:, 1] == a2))[0][0])
-            ib2 = i0 + int(np.where((bl[:, 0] == a1) & (bl[:, 1] == a3))[0][0])
-            ib3 = i0 + int(np.where((bl[:, 0] == a2) & (bl[:, 1] == a3))[0][0])
-            ph = phase[ib1] + phase[ib2] - phase[ib3]
-            cphs.append(np.arctan2(np.sin(ph), np.cos(ph)))
-            cpix.append((ib1, ib2, ib3))
-            trid.append(a1 + PK3I * (a2 + PK3I * a3))
-            tcp.append(tsec[i0])
-    return (np.array(cphs, np.float32), np.array(cpix, np.int32).reshape(-1, 3),
-            np.array(trid, np.int32), np.array(tcp, float))
+        na = ant.size
+        if na < 3:
+            continue
+        slot = np.searchsorted(ant, bl)
+        key = slot[:, 0] * na + slot[:, 1]
+        ukey, first = np.unique(key, return_index=True)   # first row of each baseline
+        row = np.full(na * na, -1, np.int64)
+        row[ukey] = i0 + first
+        tri = _triangle_slots(na)
+        ib1 = row[tri[:, 0] * na + tri[:, 1]]
+        ib2 = row[tri[:, 0] * na + tri[:, 2]]
+        ib3 = row[tri[:, 1] * na + tri[:, 2]]
+        if (ib1 < 0).any() or (ib2 < 0).any() or (ib3 < 0).any():
+            raise IndexError("calc_closures: a triangle of the span at rows %d-%d lacks one of "
+                             "its baselines" % (i0, i1 - 1))
+        ph = phase[ib1] + phase[ib2] - phase[ib3]
+        cphs.append(np.arctan2(np.sin(ph), np.cos(ph)))
+        cpix.append(np.stack([ib1, ib2, ib3], 1))
+        a = ant[tri]
+        trid.append(a[:, 0] + PK3I * (a[:, 1] + PK3I * a[:, 2]))
+        tcp.append(np.full(tri.shape[0], tsec[i0], float))
+    if not cphs:
+        return empty
+    return (np.concatenate(cphs).astype(np.float32),
+            np.concatenate(cpix).astype(np.int32).reshape(-1, 3),
+            np.concatenate(trid).astype(np.int32), np.concatenate(tcp))
 
 
 def count_lines(filename, numcount=None):

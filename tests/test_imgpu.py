@@ -10,10 +10,36 @@ import os
 import numpy as np
 import pytest
 
+import itertools
+
 import oracle
 from cuda_mcmc_gb300 import imgpu, synth
+from oracle.ref_build import REF_ROOT
 
-REF_UV = sorted(glob.glob("/root/reference/examples/sgra_model_fit/*_uvdata.txt"))
+REF_UV = sorted(glob.glob(os.path.join(REF_ROOT, "examples", "sgra_model_fit", "*_uvdata.txt")))
+
+
+def _closures_loop(phase, tsec, blin):
+    """The reference's triangle loop (src/imgpu.py:1229-1325) restated
+    literally: per equal-time span, every combination of its sorted
+    antennas, each baseline's first row found by search."""
+    ibeg, iend = imgpu.get_time_indices(tsec)
+    cphs, cpix, trid, tcp = [], [], [], []
+    bls = np.asarray(blin)
+    for i0, i1 in zip(ibeg, iend):
+        bl = bls[i0:i1].astype(int)
+        ant = np.unique(bl)
+        for a1, a2, a3 in (ant[list(t)] for t in itertools.combinations(range(ant.size), 3)):
+            ib1 = i0 + int(np.where((bl[:, 0] == a1) & (bl[:, 1] == a2))[0][0])
+            ib2 = i0 + int(np.where((bl[:, 0] == a1) & (bl[:, 1] == a3))[0][0])
+            ib3 = i0 + int(np.where((bl[:, 0] == a2) & (bl[:, 1] == a3))[0][0])
+            ph = phase[ib1] + phase[ib2] - phase[ib3]
+            cphs.append(np.arctan2(np.sin(ph), np.cos(ph)))
+            cpix.append((ib1, ib2, ib3))
+            trid.append(a1 + imgpu.PK3I * (a2 + imgpu.PK3I * a3))
+            tcp.append(tsec[i0])
+    return (np.array(cphs, np.float32), np.array(cpix, np.int32).reshape(-1, 3),
+            np.array(trid, np.int32), np.array(tcp, float))
 
 
 def _wrap(x):
@@ -48,6 +74,35 @@ def test_calc_closures_triangles(tmp_path):
     assert np.all(blin[cpix[:, 1], 1] == blin[cpix[:, 2], 1])
 
 
+def test_calc_closures_matches_the_reference_loop():
+    """Spans with different antenna sets, a repeated baseline row (the first
+    one counts), spans under 3 rows (skipped) and unsorted baselines."""
+    rng = np.random.default_rng(4)
+    rows_b, rows_t = [], []
+    for it, ants in enumerate([(1, 2, 3, 4, 5), (2, 3, 5, 7), (1, 3), (1, 2, 4, 6, 8, 9)]):
+        bl = [(a, b) for a, b in itertools.combinations(ants, 2)]
+        rng.shuffle(bl)
+        if it == 0:
+            bl.append(bl[0])                      # repeated baseline: first row wins
+        rows_b += bl
+        rows_t += [1000.0 + 60 * it] * len(bl)
+    blin = np.array(rows_b, np.int32)
+    tsec = np.array(rows_t, np.float32)
+    phase = rng.uniform(-np.pi, np.pi, len(rows_b)).astype(np.float32)
+    got = imgpu.calc_closures(phase, tsec, blin)
+    ref = _closures_loop(phase, tsec, blin)
+    assert got[0].size == imgpu.cbinom(5, 3) + imgpu.cbinom(4, 3) + imgpu.cbinom(6, 3)
+    for g, r in zip(got[1:], ref[1:]):
+        assert np.array_equal(g, r)
+    assert np.allclose(_wrap(got[0] - ref[0]), 0, atol=2e-6)
+    # a triangle whose baseline is missing fails as the reference's loop does
+    keep = np.arange(len(rows_b)) != 1           # row 1's baseline occurs once
+    with pytest.raises(IndexError):
+        imgpu.calc_closures(phase[keep], tsec[keep], blin[keep])
+    with pytest.raises(IndexError):
+        _closures_loop(phase[keep], tsec[keep], blin[keep])
+
+
 def test_helpers():
     assert imgpu.cbinom(6, 3) == 20 and imgpu.cbinom(2, 3) == -1
     c = imgpu.combgen(6, 3)
@@ -67,6 +122,10 @@ def test_read_reference_uv_files():
         assert cphs.size > 0
         ref = phase[cpix[:, 0]] + phase[cpix[:, 1]] - phase[cpix[:, 2]]
         assert np.allclose(_wrap(cphs - ref), 0, atol=1e-5)
+        loop = _closures_loop(phase, tsec, blin)
+        for g, r in zip((cpix, trid, tcp), loop[1:]):
+            assert np.array_equal(g, r)
+        assert np.allclose(_wrap(cphs - loop[0]), 0, atol=2e-6)
 
 
 def test_mcgpu_defaults_follow_the_reference():
