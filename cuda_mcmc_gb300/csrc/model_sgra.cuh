@@ -393,9 +393,7 @@ struct SgraModel {
     // One model term per (point, replica); the points are packed closure
     // corners first, so only the first nused need a phase: each thread walks
     // its stride through [0, nused) with phases, then on without.
-    auto terms = [&](int i, auto with_phase) {
-      const float4 d = __ldg(&pk.vis[i]);
-      const float rho = __ldg(&pk.rho[i]);
+    auto terms = [&](int i, const float4 d, const float rho, auto with_phase) {
 #pragma unroll
       for (int r = 0; r < R; ++r) {
 #if !CMC_BRANCHFREE
@@ -418,15 +416,52 @@ struct SgraModel {
         }
       }
     };
+    // The next point's data is loaded one iteration ahead (its L2 latency
+    // overlaps this point's terms when the data set outgrows L1).
     const int nused = cta.model_i;
     int i = tid;
-    for (; i < nused; i += T) terms(i, std::true_type{});
-    for (; i < npts; i += T) terms(i, std::false_type{});
+    float4 dn = make_float4(0.f, 0.f, 0.f, 0.f);
+    float rn = 0.0f;
+    if (i < npts) {
+      dn = __ldg(&pk.vis[i]);
+      rn = __ldg(&pk.rho[i]);
+    }
+    auto next = [&](int i, float4 &d, float &rho) {
+      d = dn;
+      rho = rn;
+      if (i + T < npts) {
+        dn = __ldg(&pk.vis[i + T]);
+        rn = __ldg(&pk.rho[i + T]);
+      }
+    };
+    for (; i < nused; i += T) {
+      float4 d;
+      float rho;
+      next(i, d, rho);
+      terms(i, d, rho, std::true_type{});
+    }
+    for (; i < npts; i += T) {
+      float4 d;
+      float rho;
+      next(i, d, rho);
+      terms(i, d, rho, std::false_type{});
+    }
     if (pk.ncph == 0 || pk.npass < 2) return;
     __syncthreads();   // also orders the global phase stores before the reads (GL)
+    // closure indices and data one closure ahead, likewise
+    int4 qn = make_int4(0, 0, 0, 0);
+    float4 fn = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tid < pk.ncph) {
+      qn = __ldg(&pk.cli[tid]);
+      fn = __ldg(&pk.clf[tid]);
+    }
     for (int c = tid; c < pk.ncph; c += T) {
-      const int4 q = __ldg(&pk.cli[c]);
-      const float4 f = __ldg(&pk.clf[c]);
+      const int4 q = qn;
+      const float4 f = fn;
+      if (c + T < pk.ncph) {
+        qn = __ldg(&pk.cli[c + T]);
+        fn = __ldg(&pk.clf[c + T]);
+      }
 #pragma unroll
       for (int r = 0; r < R; ++r) {
 #if !CMC_BRANCHFREE
