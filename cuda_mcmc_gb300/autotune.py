@@ -31,12 +31,22 @@ _STATE = ("pcur", "chi2c", "flag", "ptent", "ptentn", "pstp", "n_acpt", "n_exch"
           "inj_cur")
 
 
+def _build_stamp(lib_file: str) -> str:
+    """The source digest the library was built from (shapes timed on other
+    kernels are not reused)."""
+    try:
+        with open(lib_file + ".stamp") as f:
+            return f.read().strip()
+    except OSError:
+        return ""
+
+
 def signature(job) -> str:
     j = job.job
     dev = torch.cuda.get_device_name(job.device)
     return "|".join(str(x) for x in (
-        os.path.basename(job.L._name), dev, j.nbeta, j.nseq, j.ndat, j.hidat[0], j.hidat[2],
-        j.nptot, j.nprm, j.npass, j.imodel, j.nadj))
+        os.path.basename(job.L._name), _build_stamp(job.L._name), dev, j.nbeta, j.nseq, j.ndat,
+        j.hidat[0], j.hidat[2], j.nptot, j.nprm, j.npass, j.imodel, j.nadj))
 
 
 def _load_file():
