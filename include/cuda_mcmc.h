@@ -172,8 +172,9 @@ size_t cmc_work_bytes(const cmc_job *job, int mode);
 
 /* Launch shape the library picks for a cmc_run of this job: replicas per
  * CTA R, cluster size G = nbeta/R, threads per CTA T, closure storage
- * (1 = unit phasors, 0 = phases), dynamic shared memory and resident
- * clusters per wave.  The reference always launches <<<nseq, nbeta>>> per
+ * (1 = unit phasors, 0 = phases in shared memory, 2 = phases in global
+ * memory, which needs job->work of cmc_work_bytes(job, 0) bytes), dynamic
+ * shared memory and resident clusters per wave.  The reference always launches <<<nseq, nbeta>>> per
  * step kernel and <<<nbeta*nseq*ndat/128+1, 128>>> for the model
  * (src/gpu_mcmc.cu:686-687). */
 int cmc_query_config(const cmc_job *job, int *R, int *G, int *T, int *phasor, size_t *smem,
