@@ -91,9 +91,16 @@ def candidates(job):
     return out
 
 
+# a measured shape replaces the library's own pick only when it is faster
+# by more than this fraction (shapes within timing noise keep the pick, so
+# that repeated tunings agree)
+MARGIN = 0.01
+
+
 def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
     """Return the fastest shape {R, T, phasor} for ``job`` (a DeviceJob) and
-    store it on the job (``job.shape``), which then applies it to every run."""
+    store it on the job (``job.shape``), which then applies it to every run.
+    The library's own pick is kept unless a shape beats it by MARGIN."""
     _load_file()
     job.shape = None
     key = signature(job)
@@ -103,6 +110,12 @@ def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
     saved = {k: job.t[k].clone() for k in _STATE if k in job.t}
     itr_done = job.itr_done
     best, best_t = None, float("inf")
+    try:
+        own = job.config()
+        own = (own["R"], own["T"], own["phasor"])
+    except _lib.McmcError:
+        own = None
+    own_t = float("inf")
     L = job.L
     try:
         for cfg in candidates(job):
@@ -124,6 +137,8 @@ def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
             t = min(times)
             if verbose:
                 print("autotune R=%d T=%d phasor=%d: %.3f ms" % (cfg["R"], cfg["T"], cfg["phasor"], t))
+            if (cfg["R"], cfg["T"], cfg["phasor"]) == own:
+                own_t = t
             if t < best_t:
                 best_t, best = t, {"R": cfg["R"], "T": cfg["T"], "phasor": cfg["phasor"]}
     finally:
@@ -134,6 +149,8 @@ def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
         torch.cuda.synchronize(job.device)
     if best is None:
         raise _lib.McmcError(_lib.CMC_ERR_UNSUPPORTED, "autotune: no launch shape ran")
+    if own is not None and own_t < float("inf") and best_t > (1.0 - MARGIN) * own_t:
+        best = {"R": own[0], "T": own[1], "phasor": own[2]}
     _CACHE[key] = best
     _save_file()
     job.shape = dict(best)

@@ -93,6 +93,14 @@ inline int smem_optin()
   return v;
 }
 
+inline long long l2_bytes()
+{
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev);
+  return v;
+}
+
 template <class Model>
 size_t plan_bytes(const cmc_job &j, const typename Model::Packed &pk, int R, int T, int sweep)
 {
@@ -126,6 +134,7 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
   const int Tfix = ov.T ? ov.T : env_int("CUDA_MCMC_THREADS", 0);
   const int Pfix = ov.phasor >= 0 ? ov.phasor : env_int("CUDA_MCMC_PHASOR", -1);
   const int lim = smem_optin();
+  const double l2_budget = 0.75 * (double)l2_bytes();
   double best = 1e300;
   bool found = false;
   const int Rs[] = {1, 2, 4, 8, 16, 32};
@@ -151,8 +160,12 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         });
         if (n <= 0) continue;
         const int waves = (j.nseq + n - 1) / n;
-        // Measured on GB300, lexicographic, lower is better.  Fewest waves of
-        // resident clusters first.  Then, with a few data terms per replica
+        // Measured on GB300, lexicographic, lower is better.  With phases in
+        // global memory, first whether the resident replicas' phase regions
+        // fit in three quarters of L2 (20000 visibilities: 36 resident
+        // clusters of 32 replicas, 92 MB, in two waves beat 64 clusters,
+        // 164 MB, in one by 7 %: the larger set spills to DRAM).  Then fewest
+        // waves of resident clusters.  Then, with a few data terms per replica
         // (the plugin models: ndat 1-8), the per-proposal serial work of a
         // CTA's R replicas is the time: fewest replicas per CTA, then fewest
         // threads (Rosenbrock, 16 x 32: R=2 T=64 4.3 ms, R=8 T=256 6.9 ms).
@@ -163,15 +176,20 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         // work per thread), except with phases in global memory, where 4
         // replicas per CTA do best (20000 visibilities: R=4 T=128 11.1 ms,
         // R=8 T=256 12.7 ms per 4 iterations).
-        double score;
+        double phase_set = 0.0;
+        if constexpr (Model::kGlobalPhases) {
+          if (ph == 2) phase_set = (double)std::min(n, j.nseq) * j.nbeta * (double)q.npts * 4.0;
+        }
+        const int spill = (ph == 2 && l2_budget > 0.0 && phase_set > l2_budget) ? 1 : 0;
+        double score = spill * 100000.0;
         if (Model::points(q) <= kFewPoints) {
-          score = waves * 1000.0 + R * 10.0 + T / 64;
+          score += waves * 1000.0 + R * 10.0 + T / 64;
         } else {
           const int tpr = T / R;
           const int shape_rank = (tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2;
           const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
           const double r_rank = (ph == 2) ? (double)std::abs(R - 4) : -(double)R;
-          score = waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 + r_rank;
+          score += waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 + r_rank;
         }
         if (score < best - 1e-9) {
           best = score;
