@@ -12,8 +12,22 @@ the reference's sources where they lie (nothing is copied into this repo):
   * oracle/ref_driver.cpp supplies the launch loops of run_mcmc /
     run_calcmodchi2 / run_calcmodel.
 
-Only this container has the reference tree; the outputs are used here to
-generate the committed golden fixtures (tests/golden/make_golden.py).
+For the same models it also builds the reference's GPU code, unchanged:
+src/gpu_mcmc.cu (all of it, with the example's model.cuh) for sm_103a as
+``oracle/_ref/ref_gpu_<name>.cubin`` and as PTX (``.ptx``, loaded by the
+driver's JIT where the cubin is absent), plus ``ref_gpu_layout.json``, the
+byte offsets of the reference's CMcmcFit members printed by
+oracle/ref_layout.cu.  oracle/ref_gpu.py loads those kernels through the CUDA
+driver API and launches them in run_mcmc's order: the reference's own CUDA
+build, run on the GPU beside this library.
+
+The reference tree is found through the environment variable
+CUDA_MCMC_REFERENCE; a build made with it records the path in
+``oracle/_ref/source_root`` so that later rebuilds in the same checkout find
+it again.  Without either, nothing is built.  Only the build container has
+the reference tree: the CPU outputs generate the committed golden fixtures
+(tests/golden/make_golden.py), and the GPU outputs (device code and a JSON
+file, no host binaries) travel with the working tree to the GPU host.
 """
 from __future__ import annotations
 
@@ -25,7 +39,18 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SHIM = os.path.join(HERE, "ref_shim")
-REF_ROOT = os.environ.get("CUDA_MCMC_REFERENCE", "/root/reference")
+_ROOT_FILE = os.path.join(OUT, "source_root")
+
+
+def _ref_root():
+    root = os.environ.get("CUDA_MCMC_REFERENCE", "")
+    if not root and os.path.isfile(_ROOT_FILE):
+        with open(_ROOT_FILE) as f:
+            root = f.read().strip()
+    return root
+
+
+REF_ROOT = _ref_root()
 
 MODELS = {"sgra": "examples/sgra_model_fit",
           "rosenbrock": "examples/search_Rosenbrock",
@@ -41,7 +66,13 @@ def _host_has_fma() -> bool:
 
 
 def available() -> bool:
-    return os.path.isfile(os.path.join(REF_ROOT, "src", "gpu_mcmc.cu"))
+    return bool(REF_ROOT) and os.path.isfile(os.path.join(REF_ROOT, "src", "gpu_mcmc.cu"))
+
+
+def _remember_root():
+    os.makedirs(OUT, exist_ok=True)
+    with open(_ROOT_FILE, "w") as f:
+        f.write(REF_ROOT + "\n")
 
 
 def lib_path(name: str) -> str:
@@ -51,7 +82,7 @@ def lib_path(name: str) -> str:
 def build(force: bool = False) -> list:
     if not available():
         return []
-    os.makedirs(OUT, exist_ok=True)
+    _remember_root()
     src = os.path.join(REF_ROOT, "src")
     # nvcc contracts a*b + c into fused multiply-adds by default (-fmad=true);
     # -ffp-contract=fast with FMA instructions gives the host build the same
@@ -82,7 +113,54 @@ def build(force: bool = False) -> list:
     return built
 
 
+# ---- the reference's GPU build --------------------------------------------------
+
+def gpu_paths(name: str) -> dict:
+    return {"cubin": os.path.join(OUT, "ref_gpu_%s.cubin" % name),
+            "ptx": os.path.join(OUT, "ref_gpu_%s.ptx" % name),
+            "layout": os.path.join(OUT, "ref_gpu_layout.json")}
+
+
+def _nvcc() -> str:
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    p = os.path.join(cuda, "bin", "nvcc")
+    return p if os.path.exists(p) else "nvcc"
+
+
+def build_gpu(force: bool = False) -> list:
+    """src/gpu_mcmc.cu + examples/<m>/model.cuh for sm_103a (cubin and PTX),
+    compiled as the reference's src/Makefile compiles it (nvcc defaults for
+    device code: -O3, fused multiply-adds), and the CMcmcFit layout."""
+    if not available():
+        return []
+    _remember_root()
+    src = os.path.join(REF_ROOT, "src")
+    out = []
+    lay = gpu_paths("sgra")["layout"]
+    if force or not os.path.exists(lay):
+        exe = os.path.join(OUT, "ref_layout")
+        subprocess.run([_nvcc(), "-std=c++17", "-w", "-I", src, "-o", exe,
+                        os.path.join(HERE, "ref_layout.cu")], check=True)
+        txt = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+        os.remove(exe)
+        with open(lay, "w") as f:
+            f.write(txt)
+    out.append(lay)
+    for name, d in MODELS.items():
+        p = gpu_paths(name)
+        inc = ["-I", src, "-I", os.path.join(REF_ROOT, d)]
+        for kind, flags in (("cubin", ["-cubin", "-arch=sm_103a"]),
+                            ("ptx", ["-ptx", "-arch=compute_103a"])):
+            if force or not os.path.exists(p[kind]):
+                subprocess.run([_nvcc(), *flags, "-w", *inc, "-o", p[kind],
+                                os.path.join(src, "gpu_mcmc.cu")], check=True)
+            out.append(p[kind])
+    return out
+
+
 if __name__ == "__main__":
     if "--clean" in sys.argv and os.path.isdir(OUT):
         shutil.rmtree(OUT)
-    print("\n".join(build(force="--force" in sys.argv)) or "reference tree not present")
+    force = "--force" in sys.argv
+    print("\n".join(build(force=force) + build_gpu(force=force))
+          or "reference tree not found (set CUDA_MCMC_REFERENCE)")

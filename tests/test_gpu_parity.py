@@ -21,7 +21,7 @@ import pytest
 import oracle
 from conftest import golden
 from cuda_mcmc_gb300 import _lib, mcmc_interf, synth
-from cuda_mcmc_gb300.device import DeviceJob
+from cuda_mcmc_gb300.device import BatchJob, DeviceJob
 
 pytestmark = pytest.mark.gpu
 
@@ -171,6 +171,71 @@ def _sgra_cpext(w, seed=12):
         icoor=np.zeros(1, np.int32), idat=np.array([nvis, 0, 1], np.int32))
 
 
+def _lockstep(cases, run_one, nburn, niter, seed=77):
+    """Lock-step harness.  ``cases`` = [(workload, job)] with injected-stream
+    jobs whose state already holds the initialised replicas (do_init run);
+    ``run_one(burn)`` runs one burn-in or main iteration of every job (one
+    launch per job, or one batch launch).  Before each iteration the FP64
+    oracle takes the kernel's state (and stream cursors), runs the same
+    iteration with the same draws, and the outcomes are compared: identical
+    decisions (acceptances, exchanges, step histories, temperatures, stream
+    positions), chi^2 within 1e-5 and parameters within float rounding.
+    An iteration that differs must contain a near tie in the oracle's trace
+    (|u - alpha| < 1e-3); at most one such iteration is allowed."""
+    mismatched = 0
+    for step in range(nburn + niter):
+        burn = step < nburn
+        runs = []
+        for w, job in cases:
+            s = job.to_numpy()
+            st = _oracle_state_from(s, w, job.niter_total)
+            ors = oracle.Streams(job.streams[0], job.streams[1], s["inj_cur"][:, 0].copy(),
+                                 s["inj_cur"][:, 1].copy())
+            tr = oracle.sweep(_pb(w), st, ors, 0, 1 if burn else 0, 0 if burn else 1, trace=True)
+            runs.append((st, ors, tr))
+        run_one(burn)
+        bad = False
+        for (w, job), (st, ors, tr) in zip(cases, runs):
+            job.check()
+            s = job.to_numpy()
+            same = (np.array_equal(s["n_acpt"], st.n_acpt) and np.array_equal(s["n_exch"], st.n_exch)
+                    and np.array_equal(s["tcur"], st.tcur) and np.array_equal(s["n_hist"], st.n_hist)
+                    and np.array_equal(s["inj_cur"][:, 0], ors.cu)
+                    and np.array_equal(s["inj_cur"][:, 1], ors.cn))
+            if same:
+                assert np.allclose(s["pcur"], st.pcur, rtol=1e-6, atol=1e-7)
+                assert np.max(np.abs(s["chi2c"] - st.chi2c) / np.maximum(st.chi2c, 1e-6)) < CHI2_RTOL
+            else:
+                # allowed only when the oracle saw a near tie in this iteration
+                alpha_m = np.abs(tr.margin[tr.dec >= 0])
+                x_m = np.abs(tr.xmargin)
+                assert alpha_m.min(initial=1.0) < TIE_RTOL or x_m.min(initial=1.0) < TIE_RTOL
+                bad = True
+        mismatched += bad
+    assert mismatched <= 1
+
+
+def _injected_job(w, niter_total, seed=77, shape=None):
+    nrep = w.nbeta * w.nseq
+    rs = oracle.make_streams(nrep, 4000, 1000, seed)
+    job = DeviceJob.from_workload(w, niter_total=niter_total, rng="injected", streams=(rs.u, rs.n))
+    job.streams = (rs.u, rs.n)
+    job.shape = shape
+    return job
+
+
+def _check_init(w, job):
+    """The kernel's init_pcur + first chi^2 against the oracle's."""
+    s = job.to_numpy()
+    st = oracle.new_state(w.pdescr, w.pmint, w.pmaxt, w.beta(), w.nseq, job.niter_total,
+                          ptotal=w.ptotal, ndat=w.ndat)
+    if w.pstp0 is not None:
+        st.pstp[:] = np.asarray(w.pstp0, np.float32)[:, None, None]
+    oracle.sweep(_pb(w), st, oracle.Streams(*job.streams), 1, 0, 0)
+    assert np.allclose(s["pcur"], st.pcur, rtol=1e-6, atol=1e-7)
+    assert np.max(np.abs(s["chi2c"] - st.chi2c) / np.maximum(st.chi2c, 1e-6)) < CHI2_RTOL
+
+
 @pytest.mark.parametrize("cfg", ["sgra", "sgra_cpext", "sgra_npass1", "sgra_nbeta64", "nlsys",
                                  "rosenbrock"])
 def test_sweep_lockstep_vs_fp64_oracle(cfg):
@@ -195,42 +260,63 @@ def test_sweep_lockstep_vs_fp64_oracle(cfg):
     else:
         w = synth.rosenbrock(nseq=2, nbeta=8)
     nburn, niter = 6, 6
-    nrep = w.nbeta * w.nseq
-    rs = oracle.make_streams(nrep, 4000, 1000, 77)
-    job = DeviceJob.from_workload(w, niter_total=niter, rng="injected", streams=(rs.u, rs.n))
+    job = _injected_job(w, niter)
     job.run(0, 0, do_init=True)
     job.check()
-    s = job.to_numpy()
-    st = oracle.new_state(w.pdescr, w.pmint, w.pmaxt, w.beta(), w.nseq, niter, ptotal=w.ptotal,
-                          ndat=w.ndat)
-    if w.pstp0 is not None:
-        st.pstp[:] = np.asarray(w.pstp0, np.float32)[:, None, None]
-    ors = oracle.Streams(rs.u, rs.n)
-    oracle.sweep(_pb(w), st, ors, 1, 0, 0)
-    assert np.allclose(s["pcur"], st.pcur, rtol=1e-6, atol=1e-7)
-    assert np.max(np.abs(s["chi2c"] - st.chi2c) / np.maximum(st.chi2c, 1e-6)) < CHI2_RTOL
-    mismatched = 0
-    for step in range(nburn + niter):
-        burn = step < nburn
-        st = _oracle_state_from(s, w, niter)
-        ors = oracle.Streams(rs.u, rs.n, s["inj_cur"][:, 0].copy(), s["inj_cur"][:, 1].copy())
-        tr = oracle.sweep(_pb(w), st, ors, 0, 1 if burn else 0, 0 if burn else 1, trace=True)
-        job.run(1 if burn else 0, 0 if burn else 1, itr0=0)
-        job.check()
-        s = job.to_numpy()
-        same = (np.array_equal(s["n_acpt"], st.n_acpt) and np.array_equal(s["n_exch"], st.n_exch)
-                and np.array_equal(s["tcur"], st.tcur) and np.array_equal(s["n_hist"], st.n_hist)
-                and np.array_equal(s["inj_cur"][:, 0], ors.cu))
-        if same:
-            assert np.allclose(s["pcur"], st.pcur, rtol=1e-6, atol=1e-7)
-            assert np.max(np.abs(s["chi2c"] - st.chi2c) / np.maximum(st.chi2c, 1e-6)) < CHI2_RTOL
-        else:
-            # allowed only when the oracle saw a near tie in this iteration
-            alpha_m = np.abs(tr.margin[tr.dec >= 0])
-            x_m = np.abs(tr.xmargin)
-            assert alpha_m.min(initial=1.0) < TIE_RTOL or x_m.min(initial=1.0) < TIE_RTOL
-            mismatched += 1
-    assert mismatched <= 1
+    _check_init(w, job)
+    _lockstep([(w, job)], lambda burn: job.run(1 if burn else 0, 0 if burn else 1, itr0=0),
+              nburn, niter)
+
+
+# Launch shapes the benchmarks run, forced through cmc_set_config:
+#   cfg3: 2000 vis + 600 closures at 32 temperatures as the 64 x 32 benchmark
+#         runs it -- R = 8 replicas per CTA, clusters of G = 4 CTAs of 256
+#         threads, phases in shared memory, the warp-parallel exchange reading
+#         chi^2 from three remote CTAs and the parameter rows pulled across
+#         the cluster;
+#   cfg4: the 20000-visibility shape, R = 4, T = 256, phases in global memory
+#         (3000 + 900 data: from 2048 points on the phases may live there);
+#   r2g16: R = 2, the largest (non-portable) cluster, G = 16, unit phasors.
+SHAPES = {
+    "cfg3_R8_T256_smem": (dict(nvis=2000, ncph=600), dict(R=8, T=256, phasor=0)),
+    "cfg4_R4_T256_global": (dict(nvis=3000, ncph=900), dict(R=4, T=256, phasor=2)),
+    "r2_g16_phasors": (dict(nvis=2000, ncph=600), dict(R=2, T=64, phasor=1)),
+}
+
+
+@pytest.mark.parametrize("name", list(SHAPES))
+def test_sweep_lockstep_benchmark_shapes(name):
+    """The benchmarked launch shapes (32 temperatures, 2 sequences, 4 + 4
+    iterations) make the FP64 oracle's decisions iteration by iteration."""
+    sizes, shape = SHAPES[name]
+    w = synth.sgra(seed=8, nseq=2, nbeta=32, **sizes)
+    job = _injected_job(w, 4, shape=shape)
+    cfg = job.config()
+    assert (cfg["R"], cfg["T"], cfg["phasor"]) == (shape["R"], shape["T"], shape["phasor"])
+    assert cfg["G"] == 32 // shape["R"]
+    job.run(0, 0, do_init=True)
+    job.check()
+    _check_init(w, job)
+    _lockstep([(w, job)], lambda burn: job.run(1 if burn else 0, 0 if burn else 1, itr0=0), 4, 4)
+
+
+def test_batch_lockstep_autotuned_classes():
+    """Batched fits at their size classes' autotuned launch shapes make the
+    FP64 oracle's decisions, fit by fit, iteration by iteration."""
+    sizes = [(300, 90), (2600, 780), (5200, 1560)]
+    fits = [synth.sgra(nvis=nv, ncph=nc, seed=60 + i, nseq=2, nbeta=16)
+            for i, (nv, nc) in enumerate(sizes)]
+    jobs = [_injected_job(w, 3, seed=90 + i) for i, w in enumerate(fits)]
+    batch = BatchJob(jobs)
+    batch.autotune(iters=1)
+    for j in jobs:                   # the trials advanced the stream cursors
+        j.t["inj_cur"].zero_()
+    batch.run(0, 0, do_init=True)
+    batch.check()
+    for w, j in zip(fits, jobs):
+        _check_init(w, j)
+    _lockstep(list(zip(fits, jobs)),
+              lambda burn: batch.run(1 if burn else 0, 0 if burn else 1, itr0=0), 3, 3)
 
 
 def test_mcmc_cuda_host_abi_equals_device_api():
