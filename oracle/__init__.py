@@ -70,7 +70,7 @@ class _Problem(C.Structure):
                 ("ndat", C.c_int), ("nicoor", C.c_int), ("nidat", C.c_int),
                 ("nptot", C.c_int), ("npass", C.c_int),
                 ("coor", _fp), ("dat", _fp), ("std2r", _fp),
-                ("icoor", _ip), ("idat", _ip)]
+                ("icoor", _ip), ("idat", _ip), ("arith", C.c_int)]
 
 
 class _Streams(C.Structure):
@@ -102,6 +102,8 @@ def _declare(L):
     L.or_calc_model.restype = C.c_int
     L.or_chi2_d.argtypes = [C.POINTER(_Problem), C.c_int, _dp, _dp]
     L.or_chi2_d.restype = C.c_int
+    L.or_chi2_f32.argtypes = [C.POINTER(_Problem), C.c_int, _fp, _dp]
+    L.or_chi2_f32.restype = C.c_int
     L.or_sweep.argtypes = [C.POINTER(_Problem), C.POINTER(_SweepState),
                            C.POINTER(_Streams), C.c_int, C.c_int, C.c_int, C.c_int]
     L.or_sweep.restype = C.c_int
@@ -131,6 +133,7 @@ class Problem:
     nptot: int
     imodel: int = 1
     npass: int = 1
+    arith: int = 0          # 0: FP64 model (the checker); 1: float32, as the reference computes
     _keep: list = field(default_factory=list, repr=False)
 
     def __post_init__(self):
@@ -157,7 +160,7 @@ class Problem:
                         self.ndat, int(self.icoor.size), int(self.idat.size),
                         int(self.nptot), int(self.npass),
                         _ptr(self.coor, _fp), _ptr(self.dat, _fp), _ptr(self.std2r, _fp),
-                        _ptr(self.icoor, _ip), _ptr(self.idat, _ip))
+                        _ptr(self.icoor, _ip), _ptr(self.idat, _ip), int(self.arith))
 
 
 def sgra_vis(imodel, prm, u, v):
@@ -215,10 +218,38 @@ def chi2_d(pb: Problem, p):
     p = p.reshape(-1, pb.nptot)
     out = np.zeros(p.shape[0], np.float64)
     cp = pb.c()
-    rc = lib().or_chi2_d(C.byref(cp), p.shape[0], _ptr(p, _dp), _ptr(out, _dp))
-    if rc != OK:
-        raise ValueError("or_chi2_d failed (%d)" % rc)
+    L = lib()
+    # rows split over the host threads (ctypes releases the GIL)
+    nth = max(1, min(os.cpu_count() or 1, p.shape[0] // 8))
+    bounds = np.linspace(0, p.shape[0], nth + 1).astype(int)
+
+    def part(i):
+        a, b = bounds[i], bounds[i + 1]
+        if b <= a:
+            return OK
+        return L.or_chi2_d(C.byref(cp), int(b - a), _ptr(p[a:b], _dp), _ptr(out[a:b], _dp))
+
+    if nth == 1:
+        rcs = [part(0)]
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(nth) as ex:
+            rcs = list(ex.map(part, range(nth)))
+    if any(rc != OK for rc in rcs):
+        raise ValueError("or_chi2_d failed (%s)" % rcs)
     return out.reshape(shape)
+
+
+def chi2_f32(pb: Problem, pcur):
+    """chi^2 of parameter sets in the float32 arithmetic of the reference's
+    kernels (sgra_model9 only): float64 [nrep]."""
+    pcur = np.ascontiguousarray(pcur, np.float32)
+    nrep = pcur.size // pb.nptot
+    out = np.zeros(nrep, np.float64)
+    cp = pb.c()
+    if lib().or_chi2_f32(C.byref(cp), nrep, _ptr(pcur, _fp), _ptr(out, _dp)) != OK:
+        raise ValueError("or_chi2_f32: sgra_model9 problems only")
+    return out
 
 
 def chi2_grad_fd(pb: Problem, p, h):

@@ -23,6 +23,13 @@
  *     spmp_mcmc :426-474, adjust_steps :480-526, replica_exchange
  *     :533-626, driven in the order of run_mcmc :682-763.
  *
+ * A second arithmetic (or_problem.arith = OR_ARITH_F32, Sgr A* sgra_model9
+ * only) evaluates the model and the chi^2 sum in float32 as the reference's
+ * kernels do: float model values from float Bessel functions (j0f, j1f,
+ * jnf), float closure wrap and terms (gpu_mcmc.cu:305-323) and the serial
+ * float sum of a chi2m row (spmp_mcmc, :447-448).  The CPU baseline of the
+ * benchmark times the sweep in that arithmetic.
+ *
  * Random numbers are INJECTED: every replica ist = ibeta*nseq + iseq owns a
  * stream of uniforms in (0,1] and a stream of standard normals, consumed in
  * exactly the order in which the reference's kernels call curand_uniform()
@@ -210,6 +217,71 @@ int or_sgra_vis(int imodel, const double *prm, int n, const double *u,
     return OR_OK;
 }
 
+/* sgra_model9 in float32 arithmetic (the reference's kernels compute in
+ * float, examples/sgra_model_fit/model.cuh:322-462): the same maths as
+ * or_sgra_model9 with float operations and float Bessel functions. */
+void or_sgra_model9_f(float ul, float vl, const float *prm, float *vamp, float *vpha)
+{
+    const float pi = (float)OR_PI, pi4 = 4.0f * (float)OR_PI;
+    float Zsp = prm[0], Rex = prm[1], rq = prm[2], ecc = prm[3];
+    float fade = prm[4], gax = prm[5], aq = prm[6], gq = prm[7], th = prm[8];
+    float Rin, d, gsy, gsx, gcoef, h, h0, U, V, rho, cth, sth;
+    float ree, ime, rei = 0.0f, imi = 0.0f, Fr_re, Fr_im, Vre, Vim;
+
+    Rex = (pi / 180.0f) * (Rex / 3600.0f) * 1e3f;
+    Rin = rq * Rex;
+    d = ecc * (Rex - Rin);
+    gsy = gax * Rex;
+    gsx = aq * gsy;
+    gcoef = 2.0f * powf(pi / (2.0f * sqrtf(2.0f * logf(2.0f))), 2.0f);
+    h = (2.0f / pi) / ((Rex * Rex - Rin * Rin * (1.0f + d / Rex)) * fade
+                       + (Rex * Rex - Rin * Rin * (1.0f - d / Rex)));
+    h0 = fade * h;
+    cth = cosf(th);
+    sth = sinf(th);
+    U = ul * cth + vl * sth;
+    V = -ul * sth + vl * cth;
+    rho = sqrtf(U * U + V * V);
+    if (rho > 1e-7f) {
+        float arg = 2.0f * pi * rho, aRex = arg * Rex, r2 = rho * rho, r3 = r2 * rho;
+        float b1 = j1f(aRex);
+        ree = 0.5f * (h + h0) * Rex * b1 / rho;
+        ime = (h - h0) / pi4 * (pi * Rex * (j0f(aRex) - jnf(2, aRex)) / r2 - b1 / r3) * U;
+        if (Rin != 0.0f) {
+            float aRin = arg * Rin, c1 = j1f(aRin);
+            rei = 0.5f * (h + h0 - d * (h - h0) / Rex) * Rin * c1 / rho;
+            imi = (h - h0) / pi4 * rq * (pi * Rin * (j0f(aRin) - jnf(2, aRin)) / r2 - c1 / r3) * U;
+        }
+    } else {
+        ree = 0.5f * (h + h0) * pi * Rex * Rex;
+        ime = -0.25f * pi * pi * (h - h0) * Rex * Rex * Rex * U;
+        if (Rin != 0.0f) {
+            rei = 0.5f * (h + h0 - d * (h - h0) / Rex) * pi * Rin * Rin;
+            imi = -0.25f * pi * pi * (h - h0) * (Rin * Rin * Rin * Rin / Rex) * U;
+        }
+    }
+    if (Rin != 0.0f) {
+        float dre = cosf(2.0f * pi * d * U), dim = sinf(2.0f * pi * d * U);
+        Fr_re = ree - (rei * dre - imi * dim);
+        Fr_im = ime - (rei * dim + imi * dre);
+    } else {
+        Fr_re = ree;
+        Fr_im = ime;
+    }
+    if (gax == 0.0f || aq == 0.0f || gq == 0.0f) {
+        Vre = Zsp * Fr_re;
+        Vim = Zsp * Fr_im;
+    } else {
+        float gshift = Rin - d, ug = U * gsx, vg = V * gsy;
+        float Gamp = expf(-gcoef * (ug * ug + vg * vg));
+        float Gph = -2.0f * pi * gshift * U;
+        Vre = Zsp * ((1.0f - gq) * Fr_re + gq * Gamp * cosf(Gph));
+        Vim = Zsp * ((1.0f - gq) * Fr_im + gq * Gamp * sinf(Gph));
+    }
+    *vamp = sqrtf(Vre * Vre + Vim * Vim);
+    *vpha = atan2f(Vim, Vre);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Problem description and one replica's model row.                          */
 /* ------------------------------------------------------------------------ */
@@ -220,7 +292,10 @@ typedef struct {
     int ncoor, ndat, nicoor, nidat, nptot, npass;
     const float *coor, *dat, *std2r;
     const int *icoor, *idat;
+    int arith;                 /* OR_ARITH_F64 (checker) or OR_ARITH_F32 */
 } or_problem;
+
+enum { OR_ARITH_F64 = 0, OR_ARITH_F32 = 1 };
 
 static double wrap_angle(double x) { return atan2(sin(x), cos(x)); }
 
@@ -504,9 +579,61 @@ typedef struct {
     const float *prop_chol;  /* [nseq][nprm][nprm] */
 } or_sweep_state;
 
+/* One replica's chi^2 in float32, as calc_chi2_terms (src/gpu_mcmc.cu:273-325)
+ * over examples/sgra_model_fit/model.cuh and the serial float sum of
+ * spmp_mcmc (:447-448): sgra_model9 only.  The buffers hold the float values
+ * widened to double. */
+static int chi2_of_f32(const or_problem *pb, const float *p, double *datm_row,
+                       double *phase, int *iret, double *chi2m_row, double *out)
+{
+    const int nvis = pb->idat[0], cpext = pb->nidat > 2 ? pb->idat[2] : 0;
+    int id;
+    float sum = 0.0f;
+    for (id = 0; id < pb->ndat; id++) iret[id] = 0;
+    for (id = 0; id < nvis && id < pb->ndat; id++) {
+        float a, ph;
+        or_sgra_model9_f(pb->coor[2 * id], pb->coor[2 * id + 1], p, &a, &ph);
+        datm_row[id] = a;
+        phase[id] = ph;
+        iret[id] = 1;
+    }
+    if (pass_mask_for(pb) & 2) {
+        for (id = nvis; id < pb->ndat; id++) {
+            float cph;
+            if (cpext == 0) {
+                int c = 3 * (id - nvis);
+                cph = (float)phase[pb->icoor[c]] + (float)phase[pb->icoor[c + 1]]
+                    - (float)phase[pb->icoor[c + 2]];
+            } else {
+                int c = 4 * (id - nvis) + 2 * nvis;
+                float u1 = pb->coor[c], v1 = pb->coor[c + 1];
+                float u2 = pb->coor[c + 2], v2 = pb->coor[c + 3], a, p1, p2, p3;
+                or_sgra_model9_f(u1, v1, p, &a, &p1);
+                or_sgra_model9_f(u2, v2, p, &a, &p2);
+                or_sgra_model9_f(-(u1 + u2), -(v1 + v2), p, &a, &p3);
+                cph = p1 + p2 - p3;
+            }
+            datm_row[id] = atan2f(sinf(cph), cosf(cph));
+            iret[id] = 2;
+        }
+    }
+    for (id = 0; id < pb->ndat; id++) {
+        if (iret[id] != 0) {
+            float dif = pb->dat[id] - (float)datm_row[id];
+            if (iret[id] == 2) dif = atan2f(sinf(dif), cosf(dif));
+            chi2m_row[id] = (dif * dif) * pb->std2r[id];
+        }
+        sum += (float)chi2m_row[id];
+    }
+    *out = sum;
+    return OR_OK;
+}
+
 static int chi2_of(const or_problem *pb, const float *p, double *datm_row,
                    double *phase, int *iret, double *chi2m_row, double *out)
 {
+    if (pb->arith == OR_ARITH_F32 && pb->model == OR_MODEL_SGRA && pb->imodel == 1)
+        return chi2_of_f32(pb, p, datm_row, phase, iret, chi2m_row, out);
     int rc = model_row(pb, p, datm_row, phase, iret, pass_mask_for(pb));
     if (rc) return rc;
     *out = chi2_row(pb, datm_row, iret, chi2m_row);
@@ -738,6 +865,28 @@ done:
 }
 
 /* Size of the structs, so the ctypes mirror can check its layout. */
+/* chi^2 of nrep float parameter sets in the float32 arithmetic of
+ * chi2_of_f32 (sgra_model9 only); chi2c [nrep]. */
+int or_chi2_f32(const or_problem *pb, int nrep, const float *pcur, double *chi2c)
+{
+    int r, rc = OR_OK;
+    double *datm, *phase, *chi2m;
+    int *iret;
+    if (pb->model != OR_MODEL_SGRA || pb->imodel != 1) return OR_ERR_ARG;
+    datm = (double *)calloc((size_t)pb->ndat, sizeof(double));
+    phase = (double *)calloc((size_t)pb->ndat + 1, sizeof(double));
+    chi2m = (double *)calloc((size_t)pb->ndat, sizeof(double));
+    iret = (int *)calloc((size_t)pb->ndat, sizeof(int));
+    if (!datm || !phase || !chi2m || !iret) rc = OR_ERR_ARG;
+    for (r = 0; rc == OR_OK && r < nrep; r++)
+        rc = chi2_of_f32(pb, pcur + (size_t)r * pb->nptot, datm, phase, iret, chi2m, &chi2c[r]);
+    free(datm);
+    free(phase);
+    free(chi2m);
+    free(iret);
+    return rc;
+}
+
 int or_sizeof_problem(void) { return (int)sizeof(or_problem); }
 int or_sizeof_sweep_state(void) { return (int)sizeof(or_sweep_state); }
 int or_sizeof_streams(void) { return (int)sizeof(or_streams); }

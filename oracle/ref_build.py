@@ -158,9 +158,41 @@ def build_gpu(force: bool = False) -> list:
     return out
 
 
+# ---- the reference's Cython bridge -------------------------------------------------
+
+def cython_path() -> str:
+    return os.path.join(OUT, "mcmc_interf_ref.c")
+
+
+def build_cython(force: bool = False) -> list:
+    """src/mcmc_interf.pyx, unchanged, through Cython into C (without the
+    .pyx source lines as comments).  The C compiles wherever numpy's headers
+    and a "mcmc.h" are on the include path; the tests compile it against this
+    repository's include/mcmc.h and link it with libcmc_sgra.so, the drop-in
+    use of the bridge."""
+    if not available():
+        return []
+    try:
+        from Cython.Build import cythonize  # noqa: F401
+    except ImportError:
+        return []
+    _remember_root()
+    out = cython_path()
+    if force or not os.path.exists(out):
+        import tempfile
+        tmp = tempfile.mkdtemp()
+        pyx = os.path.join(tmp, "mcmc_interf.pyx")
+        shutil.copyfile(os.path.join(REF_ROOT, "src", "mcmc_interf.pyx"), pyx)
+        subprocess.run([sys.executable, "-m", "cython", "-3", "-X", "emit_code_comments=False",
+                        "-X", "language_level=2", pyx, "-o", out], check=True,
+                       capture_output=True)
+        shutil.rmtree(tmp)
+    return [out]
+
+
 if __name__ == "__main__":
     if "--clean" in sys.argv and os.path.isdir(OUT):
         shutil.rmtree(OUT)
     force = "--force" in sys.argv
-    print("\n".join(build(force=force) + build_gpu(force=force))
+    print("\n".join(build(force=force) + build_gpu(force=force) + build_cython(force=force))
           or "reference tree not found (set CUDA_MCMC_REFERENCE)")

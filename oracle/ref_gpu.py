@@ -77,6 +77,43 @@ def _check(rc, what):
         raise RuntimeError("%s failed: %s (%d)" % (what, (s.value or b"?").decode(), rc))
 
 
+_draws = None
+
+
+def _build_draws():
+    """Compile oracle/curand_draws.cu into oracle/_build/libcurand_draws.so."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    src = os.path.join(here, "curand_draws.cu")
+    out = os.path.join(here, "_build", "libcurand_draws.so")
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        import subprocess
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        tmp = out + ".tmp%d" % os.getpid()
+        subprocess.run([ref_build._nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O2",
+                        "-shared", "-Xcompiler", "-fPIC", "-o", tmp, src], check=True)
+        os.replace(tmp, out)
+    return out
+
+
+def next_uniforms(states, per):
+    """The next ``per`` uniforms of every cuRAND XORWOW state in the device
+    tensor ``states`` [..., 48] (uint8), as a float32 array [n, per]; the
+    states are left unchanged."""
+    global _draws
+    import torch
+    if _draws is None:
+        _draws = C.CDLL(_build_draws())
+        _draws.cd_next_uniforms.restype = C.c_int
+    st = states.contiguous()
+    n = st.numel() // 48
+    out = torch.empty((n, per), dtype=torch.float32, device=st.device)
+    rc = _draws.cd_next_uniforms(C.c_void_p(st.data_ptr()), n, per, C.c_void_p(out.data_ptr()),
+                                 C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise RuntimeError("cd_next_uniforms: CUDA error %d" % rc)
+    return out.cpu().numpy()
+
+
 class _Module:
     """The reference's kernels of one model, loaded into the current context."""
 
@@ -197,7 +234,7 @@ class RefGpuJob:
                      "pout", "tout", "chi2", "tcur", "n_acpt", "n_exch", "n_cnt", "n_hist",
                      "pstp", "beta", "ptent", "ptentn"):
             put_p(name, t[name])
-        self.mc = torch.tensor(np.frombuffer(bytes(img), np.uint8), device=dev)
+        self.mc = torch.tensor(np.frombuffer(bytes(img), np.uint8).copy(), device=dev)
         self._mcp = C.c_uint64(self.mc.data_ptr())
         self.nblocks = nrep * self.ndat // BLOCKSIZE + 1
         self.launches = 0
@@ -232,6 +269,69 @@ class RefGpuJob:
             if burn:
                 self._launch("adjust_steps", self.nseq, self.nbeta)
         self._launch("replica_exchange", self.nseq, 1, 1 if burn else 0, int(itr))
+
+    def iteration_trace(self, burn, itr, chi2_rtol=1e-5, floor=1e-3):
+        """iteration() launched kernel by kernel, reading the decision inputs
+        in between: for each Metropolis decision of spmp_mcmc
+        (src/gpu_mcmc.cu:426-474) its acceptance probability alpha from the
+        chi2m row the reference just computed and the uniform u its
+        generator gives next, and likewise for every exchange attempt of
+        replica_exchange (:533-626).  A decision compares u with
+        alpha = min(1, e^x), x = -beta/2 (chi2_new - chi2_cur) (exchange:
+        -(beta_k+1 - beta_k)/2 (chi2_k - chi2_k+1)); chi^2 values that differ
+        by a relative ``chi2_rtol`` move x by up to
+        w = |beta|/2 chi2_rtol (|chi2_new| + |chi2_cur|).  Returns per
+        sequence the smallest |ln u - x| / max(w, floor) over its decisions
+        (inf where none was taken): below 1, float32 chi^2 rounding within
+        the tolerance may flip that decision."""
+        torch = self.torch
+        nb, ns = self.nbeta, self.nseq
+        old_err = np.seterr(over="ignore")
+        beta = self.t["beta"].cpu().numpy()
+        best = np.full(ns, np.inf)
+        for _ in range(self.nprm):
+            self._launch("gen_proposal", ns, nb)
+            self._chi2_terms()
+            torch.cuda.synchronize()
+            flag = self.t["flag"].cpu().numpy()
+            c2c = self.t["chi2c"].cpu().numpy()
+            rows = self.t["chi2m"].cpu().numpy()
+            c2 = np.cumsum(rows, axis=-1, dtype=np.float32)[..., -1]   # the serial float sum
+            u = next_uniforms(self.t["rndst"], 1).reshape(nb, ns).astype(np.float64)
+            x = -0.5 * beta[:, None].astype(np.float64) * (c2.astype(np.float64) - c2c)
+            wdt = 0.5 * beta[:, None] * chi2_rtol * (np.abs(c2) + np.abs(c2c))
+            m = np.abs(np.log(u) - x) / np.maximum(wdt, floor)
+            m = np.where(flag != 0, m, np.inf)
+            best = np.minimum(best, m.min(axis=0))
+            self._launch("spmp_mcmc", ns, nb)
+            if burn:
+                self._launch("adjust_steps", ns, nb)
+        torch.cuda.synchronize()
+        c2c = self.t["chi2c"].cpu().numpy()
+        extra = 8
+        us = next_uniforms(self.t["rndst"][0], 2 * nb + extra)        # replica ibeta = 0
+        for q in range(ns):
+            chi = c2c[:, q].copy()
+            pos = 0
+            for _ in range(nb):
+                while True:
+                    k = int(np.float32(nb - 1) * us[q, pos])
+                    pos += 1
+                    if k < nb - 1 or pos >= us.shape[1] - 1:
+                        break
+                db = float(beta[k + 1]) - float(beta[k])
+                x = -0.5 * db * (float(chi[k]) - float(chi[k + 1]))
+                a = np.float32(np.exp(np.float32(-0.5) * (beta[k + 1] - beta[k]) * (chi[k] - chi[k + 1])))
+                alpha = min(a, np.float32(1.0))
+                u = us[q, pos]
+                pos += 1
+                wdt = 0.5 * abs(db) * chi2_rtol * (abs(float(chi[k])) + abs(float(chi[k + 1])))
+                best[q] = min(best[q], abs(np.log(float(u)) - x) / max(wdt, floor))
+                if u <= alpha:
+                    chi[k], chi[k + 1] = chi[k + 1], chi[k]
+        self._launch("replica_exchange", ns, 1, 1 if burn else 0, int(itr))
+        np.seterr(**old_err)
+        return best
 
     def run(self, nburn, niter):
         """run_mcmc: init, nburn burn-in and niter main iterations."""

@@ -99,3 +99,35 @@ def test_injected_stream_exhaustion_is_reported():
     rs = oracle.make_streams(2, 6, 2, 1)
     with pytest.raises(RuntimeError, match="exhausted"):
         oracle.sweep(pb, st, rs, 1, 5, 5)
+
+
+@pytest.mark.parametrize("name", ["sgra_modchi2_m9.npz", "sgra_modchi2_cpext.npz"])
+def test_float32_port_matches_reference_chi2(name):
+    """The float32 arithmetic of the CPU baseline (oracle.c OR_ARITH_F32)
+    gives the reference's own float chi^2 (golden fixtures) and the FP64
+    chi^2 to float32 accuracy."""
+    g = golden(name)
+    P = g["pcur"]
+    pb = oracle.Problem("sgra", g["coor"], g["dat"], g["std2r"], g["icoor"], g["idat"],
+                        P.shape[1], int(g["imodel"]), 2, arith=1)
+    c32 = oracle.chi2_f32(pb, P)
+    assert np.max(np.abs(c32 - g["chi2c"]) / g["chi2c"]) < 1e-5
+    _, _, _, c64 = oracle.calc_modchi2(pb, P)
+    assert np.max(np.abs(c32 - c64) / c64) < 1e-5
+
+
+def test_float32_sweep_makes_the_fp64_decisions():
+    """The CPU baseline's sweep (float32 model) takes the FP64 checker's
+    decisions on the same injected streams."""
+    w = synth.sgra(nvis=300, ncph=90, seed=4, nseq=2, nbeta=8)
+    out = []
+    for arith in (0, 1):
+        pb = oracle.Problem(w.model, w.coor, w.dat, w.std2r, w.icoor, w.idat, w.nptot,
+                            w.imodel, w.npass, arith=arith)
+        st = oracle.new_state(w.pdescr, w.pmint, w.pmaxt, w.beta(), w.nseq, 4,
+                              ptotal=w.ptotal, ndat=w.ndat)
+        oracle.sweep(pb, st, oracle.make_streams(16, 2000, 500, 3), 1, 4, 4)
+        out.append(st)
+    for f in ("n_acpt", "n_exch", "tcur", "n_hist"):
+        assert np.array_equal(getattr(out[0], f), getattr(out[1], f)), f
+    assert np.max(np.abs(out[0].chi2c - out[1].chi2c) / out[0].chi2c) < 1e-5
