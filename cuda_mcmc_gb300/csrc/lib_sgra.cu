@@ -16,14 +16,21 @@
 // cudaMalloc there fails or fragments that pool), or a latency-critical
 // pipeline that cannot let cudaMalloc / cudaFree synchronise the device between
 // its stages.  cmc_run_noalloc is cmc_run with that scratch taken from a fixed
-// array compiled into this library (kStaticWorkBytes = 4 MiB, enough for about
-// 80,000 visibility + triangle points with their closures).  It calls no
-// cudaMalloc, cudaFree or other allocating routine.
+// array compiled into this library (kStaticWorkBytes = 4 MiB).  The packed
+// data takes 52 bytes per point and 32 per closure, so at most about 80,000
+// points; the closure phases of all replicas then need the rest of the array
+// (nbeta*nseq*points*4 bytes, used from 2048 points on) or, failing that,
+// shared memory (R*points*4 bytes per CTA, R >= nbeta/16: up to about 27,000
+// points at 32 temperatures).  Where cmc_run with a full job->work would keep
+// the phases in global memory and they do not fit in the array, this call
+// keeps them in shared memory, so its launch shape and speed can differ from
+// cmc_run's.  It calls no cudaMalloc, cudaFree or other allocating routine.
 //
 // The array's device address is looked up once per device, by the first call
 // made with that device current (so that first call should come before any
-// stream capture).  Every GPU that loads this library keeps the 4 MiB until
-// the process exits.  All calls share the one array and it keeps the last
+// stream capture), and cached for the life of the process: after a
+// cudaDeviceReset the cached address is stale.  Every GPU that loads this
+// library keeps the 4 MiB until the process exits.  All calls share the one array and it keeps the last
 // call's contents; nothing in it needs to start at zero (each call rewrites
 // every element it reads).  Calls that overlap on the GPU race on it: issue
 // them on one stream, or otherwise order them.
@@ -67,6 +74,26 @@ extern "C" int cmc_run_noalloc(const cmc_job *job, void *stream)
   cmc_job j = *job;
   j.work = p;
   j.work_bytes = kStaticWorkBytes;
+  // The closure phases of every replica must fit too: beside the packed data
+  // in the array (from 2048 points on, when nbeta*nseq*points floats fit
+  // there) or else in shared memory, where each CTA keeps the phases of its
+  // R >= nbeta/16 replicas.  A job that fits neither is refused here with a
+  // message that names the array.
+  {
+    int rc = cmc::validate_common(j, 0);
+    if (rc) return rc;
+    cmc::SgraModel::Packed pk;
+    const char *err = nullptr;
+    rc = cmc::SgraModel::host_dims(j, 0, pk, &err);
+    if (rc) return cmc::fail(rc, err);
+    cmc::LaunchCfg c;
+    if (cmc::pick_sweep_config<cmc::SgraModel>(j, pk, c) != CMC_OK)
+      return cmc::fail(CMC_ERR_UNSUPPORTED,
+                       "cmc_run_noalloc: the closure phases of this job fit neither beside "
+                       "the packed data in the fixed 4 MiB array (nbeta*nseq*points*4 bytes) "
+                       "nor in shared memory (R*points*4 bytes per CTA with R >= nbeta/16 "
+                       "replicas); use cmc_run with job->work of cmc_work_bytes() bytes");
+  }
   return cmc::run_sweep<cmc::SgraModel>(j, (cudaStream_t)stream);
 }
 

@@ -100,11 +100,18 @@ int cmc_run(const cmc_job *job, void *stream);
 /* libcmc_sgra.so only.  No counterpart in the reference.  cmc_run for callers
  * that cannot allocate device memory at run time (their memory is reserved
  * up front by another allocator, or a cudaMalloc / cudaFree would synchronise
- * a latency-critical pipeline): job->work is ignored and the packed-data
- * scratch comes from a fixed 4 MiB array inside the library instead (about
- * 80,000 points; larger jobs are rejected with CMC_ERR_ARG).  The array's
- * address is resolved by the first call on each device, which should come
- * before any stream capture; all calls share the array, so calls that
+ * a latency-critical pipeline): job->work is ignored and the scratch comes
+ * from a fixed 4 MiB array inside the library instead.  Limits: the packed
+ * data (52 bytes per point + 32 per closure: at most about 80,000 points,
+ * else CMC_ERR_ARG), and the closure phases of all replicas either beside it
+ * in the array (nbeta*nseq*points*4 bytes, from 2048 points on) or else in
+ * shared memory (R*points*4 bytes per CTA with R >= nbeta/16: up to about
+ * 27,000 points at 32 temperatures), else CMC_ERR_UNSUPPORTED.  A large job
+ * whose phases cmc_run would keep in a full job->work may therefore run here
+ * with its phases in shared memory, at another launch shape and speed.  The
+ * array's address is resolved by the first call on each device, which should
+ * come before any stream capture, and cached for the life of the process (it
+ * is stale after a cudaDeviceReset); all calls share the array, so calls that
  * overlap on the GPU race. */
 int cmc_run_noalloc(const cmc_job *job, void *stream);
 
