@@ -199,6 +199,29 @@ class DeviceJob:
                 self.L.cmc_set_config(0, 0, -1)
         self.itr_done = j.itr0 + j.niter
 
+    def graph_schedule(self, nburn, niter, chunk=256, itr0=0):
+        """Capture a sweep schedule of this job as ONE CUDA graph: nburn
+        burn-in iterations, then niter recorded ones (columns itr0 ..), as
+        launches of at most ``chunk`` iterations.  Replaying the graph once
+        runs the schedule from the job's current state (the launch shape and
+        the packed data are fixed at capture)."""
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.graph(g, stream=side):
+            done = 0
+            while done < nburn:
+                n = min(chunk, nburn - done)
+                self.run(n, 0, itr0=itr0, stream=side)
+                done += n
+            done = 0
+            while done < niter:
+                n = min(chunk, niter - done)
+                self.run(0, n, itr0=itr0 + done, stream=side)
+                done += n
+        self.itr_done = itr0 + niter
+        return g
+
     def autotune(self, **kw):
         """Time every feasible launch shape on this job and keep the fastest."""
         from . import autotune

@@ -130,16 +130,21 @@ def fisher_setup(job, obj, polish_iter=200, restart=True, seed=0):
     return p_star, F
 
 
-def run_fisher(job, obj, nburn, niter, first=0.25, **kw):
+def run_fisher(job, obj, nburn, niter, first=0.25, graph=False, chunk=500, **kw):
     """Fisher schedule with the same iteration budget as :func:`run_plain`
     (see the module docstring): ``first`` of the burn-in with the reference's
     proposals, then :func:`fisher_setup`, the rest of the burn-in and the
-    recorded iterations with block proposals.  Returns (p*, F)."""
+    recorded iterations with block proposals -- with ``graph``, that rest of
+    the schedule captured as one CUDA graph of launches of at most ``chunk``
+    iterations and replayed once.  Returns (p*, F)."""
     n1 = int(round(first * nburn))
     job.run(n1, 0, do_init=True)
     out = fisher_setup(job, obj, **kw)
-    job.run(nburn - n1, 0)
-    job.run(0, niter, itr0=0)
+    if graph:
+        job.graph_schedule(nburn - n1, niter, chunk=chunk, itr0=0).replay()
+    else:
+        job.run(nburn - n1, 0)
+        job.run(0, niter, itr0=0)
     return out
 
 
