@@ -5,10 +5,12 @@ one C-ABI object (lib_sgra.cu or lib_plugin.cu) plus one kernel-instance
 object per replicas-per-CTA count R (inst_*.cu with -DCMC_R=R); all objects
 of all libraries compile in parallel.
 
-Built-in libraries: ``sgra`` (the fast Sgr A* path) and the model.cuh plugins
-shipped in cuda_mcmc_gb300/models/ (rosenbrock, solvsys, nlsys).  Any other
-plugin -- e.g. a reference example's model.cuh -- is built with
-:func:`build_plugin`.
+Built-in libraries: ``sgra`` (the fast Sgr A* path), the model.cuh plugins
+shipped in cuda_mcmc_gb300/models/ (rosenbrock, solvsys, nlsys) and
+``module``, the plugin C-ABI whose kernels come from a CUDA module file
+loaded at run time (a model.cuh compiled elsewhere with
+:func:`build_module`).  Any other plugin -- e.g. a reference example's
+model.cuh -- is built with :func:`build_plugin`.
 """
 from __future__ import annotations
 
@@ -69,6 +71,12 @@ def _jobs_for(name, plugin_file=None):
     """(object path, nvcc args) for every object of one library."""
     jobs = []
     defs = []
+    if name == "module":
+        defs = ['-DCMC_PLUGIN_NAME="module"']
+        for src, tag in (("lib_plugin.cu", "abi"), ("inst_module.cu", "launch")):
+            o = os.path.join(OBJ_DIR, "module_%s.o" % tag)
+            jobs.append((o, [nvcc(), *_flags(), *defs, "-c", os.path.join(CSRC, src), "-o", o]))
+        return jobs
     if plugin_file is not None:
         defs = ['-DCMC_PLUGIN_FILE="%s"' % os.path.abspath(plugin_file),
                 '-DCMC_PLUGIN_NAME="%s"' % name]
@@ -92,13 +100,31 @@ def _run(cmd):
 
 def build(names=None, force: bool = False, jobs: int = 0, verbose: bool = False) -> dict:
     """Build the built-in libraries (all by default); returns {name: path}."""
-    names = list(names) if names else ["sgra", *BUILTIN_PLUGINS]
+    names = list(names) if names else ["sgra", *BUILTIN_PLUGINS, "module"]
     os.makedirs(OBJ_DIR, exist_ok=True)
     plan = {}
     for n in names:
-        plugin = None if n == "sgra" else os.path.join(MODELS_DIR, "%s.cuh" % n)
+        plugin = None if n in ("sgra", "module") else os.path.join(MODELS_DIR, "%s.cuh" % n)
         plan[n] = (plugin, _jobs_for(n, plugin))
     return _build_plan(plan, force, jobs, verbose)
+
+
+def build_module(model_cuh: str, out: str, ptx: bool = False, max_r: int = 32) -> str:
+    """Compile a model.cuh (reference plugin convention, unchanged) with
+    module_plugin.cu into a CUDA module file (cubin, or PTX with ``ptx``)
+    that libcmc_module.so loads at run time (cmc_module_set), with kernels
+    for 1 .. max_r replicas per CTA."""
+    if not os.path.isfile(model_cuh):
+        raise FileNotFoundError(model_cuh)
+    kind = ["-ptx", "-arch=compute_103a"] if ptx else ["-cubin", "-arch=sm_103a"]
+    os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
+    tmp = out + ".tmp%d" % os.getpid()
+    _run([nvcc(), *kind, "-O3", "-std=c++17", "-I", CSRC, "-I", INCLUDE,
+          "--expt-relaxed-constexpr", "-w",
+          '-DCMC_PLUGIN_FILE="%s"' % os.path.abspath(model_cuh), "-DCMC_MODULE_MAX_R=%d" % max_r,
+          os.path.join(CSRC, "module_plugin.cu"), "-o", tmp])
+    os.replace(tmp, out)
+    return out
 
 
 def build_plugin(model_cuh: str, name: str, force: bool = False, jobs: int = 0) -> str:

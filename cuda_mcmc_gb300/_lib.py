@@ -132,6 +132,9 @@ def _declare(L):
         L.cmc_fisher_work_bytes.restype = C.c_size_t
         L.cmc_fisher.argtypes = [C.POINTER(CmcJob), C.c_void_p, C.c_void_p]
         L.cmc_fisher.restype = C.c_int
+    if hasattr(L, "cmc_module_set"):    # module library only
+        L.cmc_module_set.argtypes = [C.c_char_p]
+        L.cmc_module_set.restype = C.c_int
     if L.cmc_sizeof_job() != C.sizeof(CmcJob):
         raise RuntimeError("cmc_job layout mismatch between %s and _lib.CmcJob" % L._name)
 
@@ -155,10 +158,31 @@ def load(model: str = "sgra", build: bool = True):
     """Load the built-in library of ``model`` (sgra, rosenbrock, solvsys, nlsys),
     building it first when ``build`` is true and it is out of date."""
     path = _build.lib_path(model)
-    if build and (model == "sgra" or model in _build.BUILTIN_PLUGINS):
+    if build and (model in ("sgra", "module") or model in _build.BUILTIN_PLUGINS):
         if not os.path.exists(path) or not os.path.exists(path + ".stamp"):
             _build.build([model])
     return load_path(path, model)
+
+
+def load_module(module_file: str, tag: str = None):
+    """A model library whose kernels come from ``module_file`` (a cubin or
+    PTX built by _build.build_module from a model.cuh): a private copy of
+    libcmc_module.so is loaded (each copy holds one module), pointed at the
+    file and returned."""
+    import shutil
+    import tempfile
+    src = _build.lib_path("module")
+    if not os.path.exists(src) or not os.path.exists(src + ".stamp"):
+        _build.build(["module"])
+    tag = tag or os.path.splitext(os.path.basename(module_file))[0]
+    d = os.path.join(tempfile.gettempdir(), "cmc_module_%d" % os.getpid())
+    os.makedirs(d, exist_ok=True)
+    dst = os.path.join(d, "libcmc_module_%s.so" % tag)
+    if not os.path.exists(dst):
+        shutil.copyfile(src, dst)
+    L = load_path(dst, tag)
+    check(L, L.cmc_module_set(os.path.abspath(module_file).encode()))
+    return L
 
 
 def check(L, rc):

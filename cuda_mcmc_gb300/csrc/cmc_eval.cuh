@@ -14,8 +14,8 @@
 namespace cmc {
 
 template <class Model, int R>
-__global__ void __launch_bounds__(kMaxThreads)
-eval_kernel(const cmc_job job, const typename Model::Packed pk, int mode)
+__device__ __forceinline__ void eval_body(const cmc_job &job, const typename Model::Packed &pk,
+                                          int mode)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
@@ -78,6 +78,13 @@ eval_kernel(const cmc_job job, const typename Model::Packed pk, int mode)
     for (int w = 0; w < NW; ++w) s += s_red[tid * NW + w];
     job.chi2c[blockIdx.x * R + tid] = s;
   }
+}
+
+template <class Model, int R>
+__global__ void __launch_bounds__(kMaxThreads)
+eval_kernel(const cmc_job job, const typename Model::Packed pk, int mode)
+{
+  eval_body<Model, R>(job, pk, mode);
 }
 
 }  // namespace cmc

@@ -93,6 +93,14 @@ inline int smem_optin()
   return v;
 }
 
+inline int sm_count()
+{
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  return v > 0 ? v : 1;
+}
+
 inline long long l2_bytes()
 {
   int dev = 0, v = 0;
@@ -185,8 +193,15 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         if (Model::points(q) <= kFewPoints) {
           score += waves * 1000.0 + R * 10.0 + T / 64;
         } else {
+          // A job whose replicas at 64 threads each fill at most half of the
+          // GPU's thread slots (few sequences) runs faster with 64 threads
+          // per replica (2000 + 600 data, 8 x 32: R=4 T=256 2.8e7 evals/s,
+          // R=8 T=256 1.7e7; 2 x 32: 6.9e6 and 4.3e6); otherwise about 32.
+          const bool small = (double)j.nseq * j.nbeta * 64.0 <= (double)sm_count() * 1024.0;
           const int tpr = T / R;
-          const int shape_rank = (tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2;
+          const int shape_rank =
+              small ? ((tpr == 64) ? 0 : (tpr == 32 || tpr == 128) ? 1 : 2)
+                    : ((tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2);
           const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
           const double r_rank = (ph == 2) ? (double)std::abs(R - 4) : -(double)R;
           score += waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 + r_rank;

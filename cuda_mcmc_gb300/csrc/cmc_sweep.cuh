@@ -474,14 +474,22 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   cluster.sync();
 }
 
-// One launch for one job: cluster c runs sequence c.
+// One launch for one job: cluster c runs sequence c.  (The kernel bodies are
+// device functions so that a model compiled into a loadable module can wrap
+// them in kernels of its own; see module_plugin.cu.)
 template <class Model, int R>
-__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
-sweep_kernel(const cmc_job job, const typename Model::Packed pk)
+__device__ __forceinline__ void sweep_body(const cmc_job &job, const typename Model::Packed &pk)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   cg::cluster_group cluster = cg::this_cluster();
   run_sequence<Model, R>(job, pk, blockIdx.x / (int)cluster.num_blocks(), cluster, smem);
+}
+
+template <class Model, int R>
+__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
+sweep_kernel(const cmc_job job, const typename Model::Packed pk)
+{
+  sweep_body<Model, R>(job, pk);
 }
 
 // Persistent launch over a work list of (job, sequence) items of many
@@ -490,9 +498,9 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
 // copies that job's descriptor into shared memory, applies this launch's
 // iteration window (do_init, nburn, niter, itr0) and runs the sequence.
 template <class Model, int R>
-__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
-batch_kernel(const cmc_job *jobs, const typename Model::Packed *pks, const int2 *items,
-             int nitems, int *counter, int do_init, int nburn, int niter, int itr0)
+__device__ __forceinline__ void batch_body(const cmc_job *jobs, const typename Model::Packed *pks,
+                                           const int2 *items, int nitems, int *counter,
+                                           int do_init, int nburn, int niter, int itr0)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ cmc_job s_job;
@@ -525,6 +533,14 @@ batch_kernel(const cmc_job *jobs, const typename Model::Packed *pks, const int2 
     __syncthreads();
     run_sequence<Model, R>(s_job, s_pk, w.y, cluster, smem);
   }
+}
+
+template <class Model, int R>
+__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
+batch_kernel(const cmc_job *jobs, const typename Model::Packed *pks, const int2 *items,
+             int nitems, int *counter, int do_init, int nburn, int niter, int itr0)
+{
+  batch_body<Model, R>(jobs, pks, items, nitems, counter, do_init, nburn, niter, itr0);
 }
 
 }  // namespace cmc

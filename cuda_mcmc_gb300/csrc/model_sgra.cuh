@@ -105,6 +105,50 @@ __device__ __forceinline__ float2 sgra_vis(const SgraFastConsts &c, const float4
   return make_float2(fmaf(ga, cg, re), fmaf(ga, sg, im));
 }
 
+// Phases kept in global memory (phase mode 2) are written and read back by
+// the same CTA within one proposal; the stores and loads carry an L2
+// evict-last policy so that the resident replicas' phase regions stay in L2
+// rather than being written back to HBM in between (CMC_PHASE_L2_HINT = 0:
+// plain stores and loads).
+#ifndef CMC_PHASE_L2_HINT
+#define CMC_PHASE_L2_HINT 1
+#endif
+__device__ __forceinline__ unsigned long long l2_evict_last_policy()
+{
+  unsigned long long pol = 0ull;
+#if CMC_PHASE_L2_HINT
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+#endif
+  return pol;
+}
+template <bool GL>
+__device__ __forceinline__ void store_phase(float *p, float v, unsigned long long pol)
+{
+#if CMC_PHASE_L2_HINT
+  if constexpr (GL) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol)
+                 : "memory");
+    return;
+  }
+#endif
+  (void)pol;
+  *p = v;
+}
+template <bool GL>
+__device__ __forceinline__ float load_phase(const float *p, unsigned long long pol)
+{
+#if CMC_PHASE_L2_HINT
+  if constexpr (GL) {
+    float v;
+    asm volatile("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol)
+                 : "memory");
+    return v;
+  }
+#endif
+  (void)pol;
+  return *p;
+}
+
 // Data packing kernels (defined once, in the library translation unit).
 __global__ void sgra_points_kernel(const float *coor, const float *dat, const float *std2r,
                                    int nvis, int ncph, int cpext, float4 *raw, float *key);
@@ -381,6 +425,7 @@ struct SgraModel {
     const float4 *btab = reinterpret_cast<const float4 *>(cta.scratch);
     float *zs = GL ? pk.gph + (size_t)cta.ph_region * npts : cta.scratch + kTabBytes / 4;
     float2 *z = reinterpret_cast<float2 *>(zs);
+    const unsigned long long pol = GL ? l2_evict_last_policy() : 0ull;
 #if !CMC_BRANCHFREE
     bool act[R];
 #pragma unroll
@@ -412,7 +457,8 @@ struct SgraModel {
           // |V| = n2 / sqrt(n2), n2 held off zero (and denormals): |V| -> 0
           const float dif = fmaf(-n2, rsqrt_ftz(fmaxf(n2, 1e-30f)), d.z);
           acc[r] = fmaf(dif * dif, d.w, acc[r]);
-          if constexpr (decltype(with_phase)::value) zs[r * npts + i] = atan2_poly(V.y, V.x);
+          if constexpr (decltype(with_phase)::value)
+            store_phase<GL>(&zs[r * npts + i], atan2_poly(V.y, V.x), pol);
         }
       }
     };
@@ -476,7 +522,9 @@ struct SgraModel {
           // residual phasor e^{i obs} * conj(m)
           dif = atan2_poly(fmaf(f.y, mr, -(f.x * mi)), fmaf(f.x, mr, f.y * mi));
         } else {
-          const float x = f.w - (zs[r * npts + q.x] + zs[r * npts + q.y] - zs[r * npts + q.z]);
+          const float x = f.w - (load_phase<GL>(&zs[r * npts + q.x], pol) +
+                                 load_phase<GL>(&zs[r * npts + q.y], pol) -
+                                 load_phase<GL>(&zs[r * npts + q.z], pol));
           dif = fmaf(-6.2831853071795865f, rintf(x * 0.15915494309189535f), x);
         }
         acc[r] = fmaf(dif * dif, f.z, acc[r]);

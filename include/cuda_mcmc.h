@@ -191,6 +191,15 @@ int cmc_query_config(const cmc_job *job, int *R, int *G, int *T, int *phasor, si
  * reference counterpart (the reference's shape is fixed). */
 void cmc_set_config(int R, int T, int phasor);
 
+/* libcmc_module.so only; no reference counterpart.  That library is the
+ * plugin C-ABI without a model compiled in: its launches take the kernels
+ * from a CUDA module file (a cubin or PTX built from a model.cuh with
+ * cuda_mcmc_gb300/csrc/module_plugin.cu), loaded at the first launch from
+ * `path` (or, without a call, from the environment variable
+ * CMC_PLUGIN_MODULE).  Call before the first launch (afterwards only the
+ * same path is accepted); returns a cmc_status. */
+int cmc_module_set(const char *path);
+
 /* Library identification; no reference counterpart. */
 const char *cmc_model_name(void);
 int cmc_abi_version(void);

@@ -158,6 +158,39 @@ def build_gpu(force: bool = False) -> list:
     return out
 
 
+# ---- the reference's model.cuh files as modules of this library ------------------
+
+PLUGIN_DIRS = {"sgra": "examples/sgra_model_fit", "rosenbrock": "examples/search_Rosenbrock",
+               "solvsys": "examples/solvsys", "template": "template"}
+
+
+def module_path(name: str) -> str:
+    return os.path.join(OUT, "plugin_%s.cubin" % name)
+
+
+def build_modules(force: bool = False) -> list:
+    """The reference's four shipped model.cuh files, unchanged, each compiled
+    with this library's module_plugin.cu (the sweep, batch and evaluation
+    kernels of the plugin path) into oracle/_ref/plugin_<name>.cubin, which
+    libcmc_module.so loads on the GPU host."""
+    if not available():
+        return []
+    _remember_root()
+    import importlib
+    sys.path.insert(0, os.path.dirname(HERE))
+    _build = importlib.import_module("cuda_mcmc_gb300._build")
+    out = []
+    for name, d in PLUGIN_DIRS.items():
+        p = module_path(name)
+        if force or not os.path.exists(p):
+            # the Sgr A* file is heavy (Bessel functions in every model call):
+            # kernels for 1 and 2 replicas per CTA keep its compile to minutes
+            _build.build_module(os.path.join(REF_ROOT, d, "model.cuh"), p,
+                                max_r=2 if name == "sgra" else 32)
+        out.append(p)
+    return out
+
+
 # ---- the reference's Cython bridge -------------------------------------------------
 
 def cython_path() -> str:
@@ -194,5 +227,6 @@ if __name__ == "__main__":
     if "--clean" in sys.argv and os.path.isdir(OUT):
         shutil.rmtree(OUT)
     force = "--force" in sys.argv
-    print("\n".join(build(force=force) + build_gpu(force=force) + build_cython(force=force))
+    print("\n".join(build(force=force) + build_gpu(force=force) + build_cython(force=force)
+                    + build_modules(force=force))
           or "reference tree not found (set CUDA_MCMC_REFERENCE)")

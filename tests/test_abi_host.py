@@ -1,7 +1,8 @@
 """CPU tests of the C-ABI libraries and the host layer (no GPU compute).
 
 * every library loads and exports every function include/cuda_mcmc.h
-  declares (cmc_run_noalloc: libcmc_sgra.so only), with the job layout the
+  declares (cmc_run_noalloc and the gradient entry points: libcmc_sgra.so
+  only; cmc_module_set: libcmc_module.so only), with the job layout the
   Python mirror expects;
 * mcmc_interf validates its arguments like the reference's Cython signatures
   (dtype / ndim errors) before anything reaches the device;
@@ -17,7 +18,7 @@ import pytest
 from cuda_mcmc_gb300 import _build, _lib, mcmc_interf, synth
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIBS = ("sgra", *_build.BUILTIN_PLUGINS)
+LIBS = ("sgra", *_build.BUILTIN_PLUGINS, "module")
 
 
 def declared_functions():
@@ -44,6 +45,8 @@ def test_library_exports_every_declared_symbol(name):
         for only_sgra in ("cmc_run_noalloc", "cmc_grad", "cmc_grad_work_bytes", "cmc_fisher",
                           "cmc_fisher_work_bytes"):
             want.discard(only_sgra)
+    if name != "module":
+        want.discard("cmc_module_set")
     assert want, "no declarations parsed"
     missing = want - syms
     assert not missing, "missing exports: %s" % sorted(missing)
