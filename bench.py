@@ -576,7 +576,7 @@ def extras(args, local, peak):
     torch.cuda.empty_cache()
     # config 5: 1024 batched fits
     out["config5_batch_1024fits"] = measure_batch(args.nfits, 3, args.warmup, False, local,
-                                                  nb=1, ni=2)
+                                                  nb=2, ni=8)
     torch.cuda.empty_cache()
     # configs 1 and 2: the plugin models
     out["config1_rosenbrock4_16x32"] = measure_plugin("rosenbrock", 2, 1, local, cpu=False)

@@ -322,9 +322,17 @@ int run_eval(const cmc_job &j, int mode, cudaStream_t s)
                                      "(give job.work cmc_work_bytes() bytes for larger data)");
   rc = Model::host_pack(j, pk, j.work, s);
   if (rc) return fail(rc, "packing the model data failed");
-  return dispatch_R<Model>(R, [&](auto rcnst) {
-    return launch_eval<Model, decltype(rcnst)::value>(j, pk, mode == 2 ? 1 : 0, T, smem, s);
-  });
+  // A count whose kernel a loaded module lacks (libcmc_module.so) reports
+  // CMC_ERR_UNSUPPORTED before launching anything: fall back to fewer
+  // replicas per CTA (the plan of R replicas also fits R/2).
+  for (; R >= 1; R /= 2) {
+    smem = plan_bytes<Model>(j, pk, R, T, 0);
+    rc = dispatch_R<Model>(R, [&](auto rcnst) {
+      return launch_eval<Model, decltype(rcnst)::value>(j, pk, mode == 2 ? 1 : 0, T, smem, s);
+    });
+    if (rc != CMC_ERR_UNSUPPORTED) return rc;
+  }
+  return rc;
 }
 
 template <class Model>
@@ -456,9 +464,14 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
     for (int R : Rs) {
       if (R > Model::kMaxR || nbeta % R || nbeta / R > 16) continue;
       const int G = nbeta / R;
-      // ~32 threads per replica, and never fewer than one thread per 16
-      // points of the class's largest job
-      const int want = std::max(32 * R, (int)std::min<long long>(256, Model::points(pk[big]) / 16));
+      // threads per replica grow with the class's data: 32, 64, then 128
+      // (measured on GB300 by BatchJob.autotune over 1024 fits of 500-50000
+      // visibilities: R=4 T=128, R=4 T=256, R=2 T=256; the larger a
+      // class's items, the more its time is the tail of its last items,
+      // which more threads per replica shorten)
+      const int tpr = 32 << std::min(c, 2);
+      const int want = tpr * R;
+      if (want > 256 && R > 1) continue;
       const int T = want <= 64 ? 64 : want <= 128 ? 128 : 256;
       for (int ph = 2; ph >= 0; --ph) {
         if (ph == 2 && !gl_all) continue;

@@ -177,7 +177,7 @@ int capacity(int kind, int R, int G, int T, size_t smem, int grid)
 int launch(int kind, int R, int G, int grid, int T, size_t smem, cudaStream_t s, void **args)
 {
   CUfunction f = function(kind, R);
-  if (!f) return CMC_ERR_CUDA;
+  if (!f) return g_mod ? CMC_ERR_UNSUPPORTED : CMC_ERR_CUDA;   // no such count / no module
   int rc = set_attrs(f, smem, G);
   if (rc) return rc;
   CUlaunchAttribute attr[1];
