@@ -464,15 +464,20 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
     for (int R : Rs) {
       if (R > Model::kMaxR || nbeta % R || nbeta / R > 16) continue;
       const int G = nbeta / R;
-      // threads per replica grow with the class's data: 32, 64, then 128
-      // (measured on GB300 by BatchJob.autotune over 1024 fits of 500-50000
-      // visibilities: R=4 T=128, R=4 T=256, R=2 T=256; the larger a
+      // Threads per replica grow with the class's data (32, 64, then 128)
+      // with 4 replicas per CTA, 2 from the third class on: the shapes
+      // BatchJob.autotune measured best on GB300 over 1024 fits of
+      // 500-50000 visibilities (R=4 T=128 phases in shared memory; R=4
+      // T=256 and R=2 T=256, phases in global memory; 1.86e7 evals/s
+      // against 1.54e7 for the most resident replicas).  The larger a
       // class's items, the more its time is the tail of its last items,
-      // which more threads per replica shorten)
+      // which more threads per replica shorten.  Other shapes rank by
+      // resident replicas, after these.
       const int tpr = 32 << std::min(c, 2);
       const int want = tpr * R;
       if (want > 256 && R > 1) continue;
       const int T = want <= 64 ? 64 : want <= 128 ? 128 : 256;
+      const bool preferred = (R == (c < 2 ? 4 : 2));
       for (int ph = 2; ph >= 0; --ph) {
         if (ph == 2 && !gl_all) continue;
         Packed q = pk[big];
@@ -484,9 +489,11 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
         });
         if (cap <= 0) continue;
         const double resident = std::min((double)cap * nbeta, (double)reps);
-        // per resident replica: phasors > phases in shared memory > phases in
-        // global memory (an L2 round trip per closure gather)
-        const double score = resident * (ph == 1 ? 1.05 : ph == 0 ? 1.0 : 0.95);
+        // the first class keeps its phases in shared memory, the larger ones
+        // in global memory (measured), then phasors
+        const double phase_pref = (c == 0) ? (ph == 0 ? 1.05 : ph == 1 ? 1.0 : 0.95)
+                                           : (ph == 2 ? 1.05 : ph == 0 ? 1.0 : 0.95);
+        const double score = (preferred ? 1e9 : 0.0) + resident * phase_pref;
         if (score > best + 1e-9) {
           best = score;
           bc.R = R; bc.G = G; bc.T = T; bc.phasor = ph; bc.smem = smem; bc.nclusters = cap;
