@@ -448,6 +448,7 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
       if (key > lo && key <= hi) mem.push_back(i);
     }
     if (mem.empty()) continue;
+    const int size_rank = (int)P->classes.size();   // 0 for the smallest non-empty class
     std::stable_sort(mem.begin(), mem.end(), [&](int a, int b) {
       return (double)npts[a] * (double)jobs[a].nseq > (double)npts[b] * (double)jobs[b].nseq;
     });
@@ -473,11 +474,11 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
       // class's items, the more its time is the tail of its last items,
       // which more threads per replica shorten.  Other shapes rank by
       // resident replicas, after these.
-      const int tpr = 32 << std::min(c, 2);
+      const int tpr = 32 << std::min(size_rank, 2);
       const int want = tpr * R;
       if (want > 256 && R > 1) continue;
       const int T = want <= 64 ? 64 : want <= 128 ? 128 : 256;
-      const bool preferred = (R == (c < 2 ? 4 : 2));
+      const bool preferred = (R == (size_rank < 2 ? 4 : 2));
       for (int ph = 2; ph >= 0; --ph) {
         if (ph == 2 && !gl_all) continue;
         Packed q = pk[big];
@@ -491,8 +492,8 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
         const double resident = std::min((double)cap * nbeta, (double)reps);
         // the first class keeps its phases in shared memory, the larger ones
         // in global memory (measured), then phasors
-        const double phase_pref = (c == 0) ? (ph == 0 ? 1.05 : ph == 1 ? 1.0 : 0.95)
-                                           : (ph == 2 ? 1.05 : ph == 0 ? 1.0 : 0.95);
+        const double phase_pref = (size_rank == 0) ? (ph == 0 ? 1.05 : ph == 1 ? 1.0 : 0.95)
+                                                   : (ph == 2 ? 1.05 : ph == 0 ? 1.0 : 0.95);
         const double score = (preferred ? 1e9 : 0.0) + resident * phase_pref;
         if (score > best + 1e-9) {
           best = score;
