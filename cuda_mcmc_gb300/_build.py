@@ -31,7 +31,7 @@ OBJ_DIR = os.path.join(LIB_DIR, "obj")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # replicas-per-CTA instances per library (must match each model's kMaxR)
-R_VALUES = {"sgra": (1, 2, 4, 8)}
+R_VALUES = {"sgra": (1, 2, 3, 4, 5, 6, 7, 8)}
 R_VALUES_PLUGIN = (1, 2, 4, 8, 16, 32)
 BUILTIN_PLUGINS = ("rosenbrock", "solvsys", "nlsys")
 

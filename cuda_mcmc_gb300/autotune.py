@@ -81,6 +81,23 @@ def candidates(job):
                     continue
                 for ph in (1, 0, 2):        # 2: phases in global memory (large data)
                     L.cmc_set_config(R, T, ph)
+                    L.cmc_set_layout(1)
+                    try:
+                        cfg = job.config()
+                    except _lib.McmcError:
+                        continue
+                    out.append(cfg)
+        # the spread layout (any R up to the model's largest, phases in
+        # shared memory; models without it report no shape)
+        for R in range(1, 9):
+            if R > job.nbeta:
+                continue
+            for T in T_VALUES:
+                if T < 32 * ((R + 31) // 32):
+                    continue
+                for ph in (1, 0):
+                    L.cmc_set_config(R, T, ph)
+                    L.cmc_set_layout(2)
                     try:
                         cfg = job.config()
                     except _lib.McmcError:
@@ -88,7 +105,12 @@ def candidates(job):
                     out.append(cfg)
     finally:
         L.cmc_set_config(0, 0, -1)
+        L.cmc_set_layout(0)
     return out
+
+
+def _key(cfg):
+    return (cfg["R"], cfg["T"], cfg["phasor"], 2 if cfg.get("layout") == "spread" else 1)
 
 
 # a measured shape replaces the library's own pick only when it is faster
@@ -111,8 +133,7 @@ def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
     itr_done = job.itr_done
     best, best_t = None, float("inf")
     try:
-        own = job.config()
-        own = (own["R"], own["T"], own["phasor"])
+        own = _key(job.config())
     except _lib.McmcError:
         own = None
     own_t = float("inf")
@@ -120,6 +141,7 @@ def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
     try:
         for cfg in candidates(job):
             L.cmc_set_config(cfg["R"], cfg["T"], cfg["phasor"])
+            L.cmc_set_layout(_key(cfg)[3])
             try:
                 job.run(0, 0, do_init=True)          # start every trial from the same state
                 job.check()
@@ -136,13 +158,16 @@ def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
                 continue
             t = min(times)
             if verbose:
-                print("autotune R=%d T=%d phasor=%d: %.3f ms" % (cfg["R"], cfg["T"], cfg["phasor"], t))
-            if (cfg["R"], cfg["T"], cfg["phasor"]) == own:
+                print("autotune R=%d T=%d phasor=%d layout=%s: %.3f ms" % (
+                    cfg["R"], cfg["T"], cfg["phasor"], cfg.get("layout"), t))
+            if _key(cfg) == own:
                 own_t = t
             if t < best_t:
-                best_t, best = t, {"R": cfg["R"], "T": cfg["T"], "phasor": cfg["phasor"]}
+                best_t, best = t, {"R": cfg["R"], "T": cfg["T"], "phasor": cfg["phasor"],
+                                   "layout": _key(cfg)[3]}
     finally:
         L.cmc_set_config(0, 0, -1)
+        L.cmc_set_layout(0)
         for k, v in saved.items():
             job.t[k].copy_(v)
         job.itr_done = itr_done
@@ -150,7 +175,7 @@ def tune(job, iters=8, repeats=2, use_cache=True, verbose=False):
     if best is None:
         raise _lib.McmcError(_lib.CMC_ERR_UNSUPPORTED, "autotune: no launch shape ran")
     if own is not None and own_t < float("inf") and best_t > (1.0 - MARGIN) * own_t:
-        best = {"R": own[0], "T": own[1], "phasor": own[2]}
+        best = {"R": own[0], "T": own[1], "phasor": own[2], "layout": own[3]}
     _CACHE[key] = best
     _save_file()
     job.shape = dict(best)

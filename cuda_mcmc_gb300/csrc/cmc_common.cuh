@@ -34,7 +34,11 @@
 namespace cmc {
 namespace cg = cooperative_groups;
 
-constexpr int kCH = 32;          // main iterations staged in smem per pout flush
+// main iterations staged in shared memory per record flush
+#ifndef CMC_KCH
+#define CMC_KCH 32
+#endif
+constexpr int kCH = CMC_KCH;
 constexpr int kMaxThreads = 256;
 constexpr int kRepF = 4;         // per-replica floats: ptent, chi2c, chi2n, beta
 constexpr int kRepI = 4;         // per-replica ints: ptentn, flag, kchosen, evaluated
@@ -156,6 +160,66 @@ __host__ __device__ inline SmemPlan make_plan(int R, int nthreads, int nptot, in
   p.scratch = o; o = align16(o + scratch_bytes);
   p.total = o;
   return p;
+}
+
+// ---- spread layout (cmc_sweep.cuh): host and device arithmetic ------------
+
+// CTA b of N over nrep replicas: first replica and count (nrep >= N).
+__host__ __device__ inline void spread_range(int nrep, int N, int b, int &start, int &cnt)
+{
+  const int q = nrep / N, rem = nrep % N;
+  cnt = q + (b < rem ? 1 : 0);
+  start = b * q + (b < rem ? b : rem);
+}
+
+// The CTA holding replica f (inverse of spread_range).
+__host__ __device__ inline int spread_cta_of(int nrep, int N, int f)
+{
+  const int q = nrep / N, rem = nrep % N, big = rem * (q + 1);
+  return f < big ? f / (q + 1) : rem + (f - big) / q;
+}
+
+// Global-memory exchange area of a spread launch (in job.work after the
+// model's scratch; spread_ctl_bytes).  The per-iteration buffers are double
+// buffered by iteration parity: a CTA rewrites a buffer two iterations later,
+// after every reader of the sequence has arrived at the iteration between.
+struct SpreadCtl {
+  int *arrive;   // [nseq] CTAs that published this launch's iterations (zeroed per launch)
+  int *done;     // [nseq] exchanges completed this launch
+  int *abort;    // [1] set when a wait ran out: every CTA stops waiting
+  float *xp;     // [2][nrep][nptot] parameters before the exchange
+  float *xc;     // [2][nrep] chi^2 before the exchange
+  int *xperm;    // [2][nrep] source temperature of each slot after the exchange
+  float *xchi;   // [2][nrep] chi^2 after the exchange
+};
+
+__host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Bytes of the SpreadCtl area; the counters (first block) are zeroed before
+// every launch.
+__host__ __device__ inline size_t spread_ctl_counter_bytes(int nseq)
+{
+  return align256(4 * (2 * (size_t)nseq + 1));
+}
+__host__ __device__ inline size_t spread_ctl_bytes(int nseq, int nbeta, int nptot)
+{
+  const size_t nrep = (size_t)nseq * nbeta;
+  return spread_ctl_counter_bytes(nseq) + align256(4 * 2 * nrep * nptot) + 3 * align256(4 * 2 * nrep);
+}
+__host__ __device__ inline SpreadCtl spread_ctl_at(unsigned char *base, int nseq, int nbeta,
+                                                   int nptot)
+{
+  const size_t nrep = (size_t)nseq * nbeta;
+  SpreadCtl c;
+  c.arrive = reinterpret_cast<int *>(base);
+  c.done = c.arrive + nseq;
+  c.abort = c.done + nseq;
+  size_t o = spread_ctl_counter_bytes(nseq);
+  c.xp = reinterpret_cast<float *>(base + o);  o += align256(4 * 2 * nrep * nptot);
+  c.xc = reinterpret_cast<float *>(base + o);  o += align256(4 * 2 * nrep);
+  c.xperm = reinterpret_cast<int *>(base + o); o += align256(4 * 2 * nrep);
+  c.xchi = reinterpret_cast<float *>(base + o);
+  return c;
 }
 
 // Per-CTA view handed to the model policies.

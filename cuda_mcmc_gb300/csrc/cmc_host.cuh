@@ -51,6 +51,7 @@ inline int cuda_fail(cudaError_t e, const char *what)
 // CUDA_MCMC_R / CUDA_MCMC_THREADS environment variables; 0 = automatic.
 struct Override {
   int R = 0, T = 0, phasor = -1;
+  int layout = 0;   // 0 = automatic, 1 = cluster layout, 2 = spread layout
 };
 inline Override &override_cfg()
 {
@@ -83,6 +84,28 @@ inline int dispatch_R(int R, F &&f)
     default: break;
   }
   return fail(CMC_ERR_UNSUPPORTED, "no kernel instance for this replicas-per-CTA count");
+}
+
+// Calls f(std::integral_constant<int, R>) for the spread-layout kernel
+// instances (R = 1..Model::kMaxR of a model with Model::kSpread).
+template <class Model, class F>
+inline int dispatch_spread_R(int R, F &&f)
+{
+  if constexpr (Model::kSpread) {
+    static_assert(Model::kMaxR <= 8, "spread instances cover R = 1..8");
+    switch (R) {
+      case 1: return f(std::integral_constant<int, 1>{});
+      case 2: return f(std::integral_constant<int, 2>{});
+      case 3: return f(std::integral_constant<int, 3>{});
+      case 4: return f(std::integral_constant<int, 4>{});
+      case 5: return f(std::integral_constant<int, 5>{});
+      case 6: return f(std::integral_constant<int, 6>{});
+      case 7: return f(std::integral_constant<int, 7>{});
+      case 8: return f(std::integral_constant<int, 8>{});
+      default: break;
+    }
+  }
+  return fail(CMC_ERR_UNSUPPORTED, "no spread-layout kernel instance for this replicas-per-CTA count");
 }
 
 inline int smem_optin()
@@ -132,21 +155,46 @@ inline bool global_phases_ok(const typename Model::Packed &pk)
 // launch-shape ranking below then minimises the work per CTA).
 constexpr int kFewPoints = 64;
 
+// The spread layout's exchange area sits in job.work after the model's
+// scratch (packed data and, when allocated, global phase regions).
+template <class Model>
+inline size_t spread_offset(const typename Model::Packed &pk)
+{
+  return align256(Model::host_work_bytes(pk));
+}
+
+// The spread layout can run this job: the model has it, every sequence's
+// exchange fits one warp (nbeta <= 32), the phases stay in shared memory
+// (pk.phasor is decided by the caller) and job.work holds the exchange area.
+template <class Model>
+inline bool spread_ok(const cmc_job &j, const typename Model::Packed &pk)
+{
+  if constexpr (!Model::kSpread) {
+    return false;
+  } else {
+    if (j.nbeta > 32 || j.work == nullptr) return false;
+    return j.work_bytes >= spread_offset<Model>(pk) + spread_ctl_bytes(j.nseq, j.nbeta, j.nptot);
+  }
+}
+
 // Pick replicas-per-CTA R (cluster size G = nbeta/R <= 16), threads T and the
 // phase storage mode by the ranking below (autotune.py measures instead).
 template <class Model>
 int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &out)
 {
+  out = LaunchCfg{};
   const Override &ov = override_cfg();
   const int Rfix = ov.R ? ov.R : env_int("CUDA_MCMC_R", 0);
   const int Tfix = ov.T ? ov.T : env_int("CUDA_MCMC_THREADS", 0);
   const int Pfix = ov.phasor >= 0 ? ov.phasor : env_int("CUDA_MCMC_PHASOR", -1);
+  const int Lfix = ov.layout ? ov.layout : env_int("CUDA_MCMC_LAYOUT", 0);
   const int lim = smem_optin();
   const double l2_budget = 0.75 * (double)l2_bytes();
   double best = 1e300;
   bool found = false;
   const int Rs[] = {1, 2, 4, 8, 16, 32};
   for (int R : Rs) {
+    if (Lfix == 2) break;   // spread layout only
     if (R > Model::kMaxR) continue;
     if (Rfix && R != Rfix) continue;
     if (j.nbeta % R != 0) continue;
@@ -215,6 +263,77 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
       }
     }
   }
+  // Spread layout (cmc_sweep.cuh): the replicas shared evenly by N
+  // co-resident CTAs.  Chosen by itself where the cluster layout's pick puts
+  // two or more CTAs on the busiest SM and the spread layout, at that pick's
+  // threads and phase storage, holds fewer replicas there (2000 + 600 data,
+  // 64 x 32 on 152 SMs: 293 CTAs of 6-7 replicas, at most 14 per SM, against
+  // 256 CTAs of 8 with up to 16; one CTA alone on an SM runs at about 0.73 of
+  // the pair's rate, so one-CTA placements are left alone).  With the layout
+  // forced (cmc_set_layout 2, the autotuner): the least-loaded spread shape
+  // in the cluster ranking's order.
+  const int sms = sm_count();
+  const int nrep = j.nbeta * j.nseq;
+  int per_sm_c = 0, load_c = 1 << 30;
+  if (found) {
+    const int wave = std::min(j.nseq, out.clusters_per_wave);
+    per_sm_c = (out.G * wave + sms - 1) / sms;
+    load_c = out.R * per_sm_c * ((j.nseq + out.clusters_per_wave - 1) / out.clusters_per_wave);
+  }
+  const bool spread_auto = found && Lfix == 0 && out.phasor != 2 && !Rfix && !Tfix &&
+                           Model::points(pk) > kFewPoints && per_sm_c >= 2;
+  if (Lfix == 2 || spread_auto) {
+    double best_s = 1e300;
+    LaunchCfg bs;
+    bool found_s = false;
+    for (int R = 1; R <= std::min(Model::kMaxR, j.nbeta); ++R) {
+      if (Rfix && R != Rfix) continue;
+      const int N = (nrep + R - 1) / R;
+      const int Ts[] = {64, 128, 256};
+      for (int T : Ts) {
+        if (Tfix && T != Tfix) continue;
+        if (spread_auto && T != out.T) continue;
+        if (T < 32 * ((R + 31) / 32)) continue;
+        for (int ph = 1; ph >= 0; --ph) {
+          if (Pfix >= 0 && ph != Pfix) continue;
+          if (spread_auto && ph != out.phasor) continue;
+          typename Model::Packed q = pk;
+          q.phasor = ph;
+          if (!spread_ok<Model>(j, q)) continue;
+          const size_t smem = plan_bytes<Model>(j, q, R, T, 1);
+          if ((long long)smem > lim) continue;
+          const int cap = dispatch_spread_R<Model>(R, [&](auto rc) {
+            return spread_capacity<Model, decltype(rc)::value>(T, smem);
+          });
+          if (cap <= 0 || N > cap || N > nrep) continue;
+          const int per_sm = (N + sms - 1) / sms;
+          const int load = R * per_sm;
+          if (spread_auto && (load >= load_c || per_sm < per_sm_c)) continue;
+          const int tpr = T / R;
+          const int shape_rank = (tpr >= 32 && tpr < 64) ? 0 : (tpr >= 16 && tpr < 128) ? 1 : 2;
+          const double score = load * 1000.0 + shape_rank * 100.0 + (ph == 1 ? 0 : 10) - R;
+          if (score < best_s - 1e-9) {
+            best_s = score;
+            bs = LaunchCfg{};
+            bs.R = R; bs.G = 0; bs.T = T; bs.phasor = ph; bs.smem = smem;
+            bs.clusters_per_wave = N;
+            bs.spread = 1;
+            bs.nblocks = N;
+            found_s = true;
+          }
+        }
+      }
+    }
+    if (found_s) {
+      out = bs;
+      found = true;
+    } else if (Lfix == 2) {
+      return fail(CMC_ERR_UNSUPPORTED,
+                  "no spread-layout launch shape fits: it needs the built-in Sgr A* model, "
+                  "nbeta <= 32, phases in shared memory, job.work of cmc_work_bytes() bytes "
+                  "and at most as many CTAs as are resident at once");
+    }
+  }
   if (!found)
     return fail(CMC_ERR_UNSUPPORTED,
                 "no sweep launch shape fits: nbeta must be a multiple of a power of two "
@@ -279,9 +398,16 @@ int run_sweep(const cmc_job &j, cudaStream_t s, LaunchCfg *used = nullptr)
   if (rc) return rc;
   rc = Model::host_pack(j, pk, j.work, s);
   if (rc) return fail(rc, "packing the model data failed");
-  rc = dispatch_R<Model>(c.R, [&](auto rcnst) {
-    return launch_sweep<Model, decltype(rcnst)::value>(j, pk, c, s);
-  });
+  if (c.spread) {
+    void *ctl = static_cast<unsigned char *>(j.work) + spread_offset<Model>(pk);
+    rc = dispatch_spread_R<Model>(c.R, [&](auto rcnst) {
+      return launch_spread<Model, decltype(rcnst)::value>(j, pk, c, ctl, s);
+    });
+  } else {
+    rc = dispatch_R<Model>(c.R, [&](auto rcnst) {
+      return launch_sweep<Model, decltype(rcnst)::value>(j, pk, c, s);
+    });
+  }
   if (used) *used = c;
   return rc;
 }
@@ -341,6 +467,11 @@ size_t work_bytes(const cmc_job &j, int mode)
   typename Model::Packed pk;
   const char *err = nullptr;
   if (Model::host_dims(j, mode, pk, &err)) return 0;
+  if constexpr (Model::kSpread) {
+    // a sweep's spread-layout exchange area after the model's scratch
+    if (mode == 0 && j.nbeta <= 32)
+      return spread_offset<Model>(pk) + spread_ctl_bytes(j.nseq, j.nbeta, j.nptot);
+  }
   return Model::host_work_bytes(pk);
 }
 

@@ -137,6 +137,54 @@ int launch_batch(const cmc_job *jobs, const typename Model::Packed *pks, const i
 }
 
 template <class Model, int R>
+int spread_capacity(int T, size_t smem)
+{
+  auto kern = spread_kernel<Model, R>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int dev = 0, coop = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return coop ? per_sm * sms : 0;
+}
+
+template <class Model, int R>
+int launch_spread(const cmc_job &j, const typename Model::Packed &pk, const LaunchCfg &c,
+                  void *ctl, cudaStream_t s)
+{
+  auto kern = spread_kernel<Model, R>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("spread kernel attributes: ") + cudaGetErrorString(e));
+  e = cudaMemsetAsync(ctl, 0, spread_ctl_counter_bytes(j.nseq), s);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("spread counters: ") + cudaGetErrorString(e));
+  const SpreadCtl x = spread_ctl_at(static_cast<unsigned char *>(ctl), j.nseq, j.nbeta, j.nptot);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.gridDim = dim3(c.nblocks);
+  cfg.blockDim = dim3(c.T);
+  cfg.dynamicSmemBytes = c.smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, j, pk, x);
+  if (e != cudaSuccess)
+    return fail(CMC_ERR_CUDA, std::string("spread kernel launch: ") + cudaGetErrorString(e));
+  return CMC_OK;
+}
+
+template <class Model, int R>
 int launch_eval(const cmc_job &j, const typename Model::Packed &pk, int model_only, int T,
                 size_t smem, cudaStream_t s)
 {
@@ -162,5 +210,12 @@ int launch_eval(const cmc_job &j, const typename Model::Packed &pk, int model_on
   template int launch_batch<MODEL, RV>(const cmc_job *, const MODEL::Packed *, const int2 *, \
                                        int, int *, int, int, size_t, int, int, int, int, int, \
                                        cudaStream_t);
+
+// The spread-layout sweep for one R (every R of 1..Model::kMaxR of a model
+// with Model::kSpread).
+#define CMC_INSTANTIATE_SPREAD(MODEL, RV)                                                  \
+  template int spread_capacity<MODEL, RV>(int, size_t);                                    \
+  template int launch_spread<MODEL, RV>(const cmc_job &, const MODEL::Packed &,           \
+                                        const LaunchCfg &, void *, cudaStream_t);
 
 }  // namespace cmc

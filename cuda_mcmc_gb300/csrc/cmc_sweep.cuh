@@ -2,6 +2,8 @@
 // The work decomposition and the reference functions it restates are
 // described at the top of cmc_common.cuh.
 #pragma once
+#include <cuda/atomic>
+
 #include "cmc_common.cuh"
 
 namespace cmc {
@@ -12,17 +14,127 @@ namespace cmc {
 #define CMC_MIN_BLOCKS 2
 #endif
 
-// One sequence iseq of `job` on the calling cluster (all its CTAs call this
-// with the same arguments).  `smem` is the CTA's dynamic shared memory, at
-// least make_plan(...).total bytes for this job.
-template <class Model, int R>
-__device__ void run_sequence(const cmc_job &job, const typename Model::Packed &pk, int iseq,
-                             cg::cluster_group &cluster, unsigned char *smem)
+// ---- replica layouts ----------------------------------------------------------
+// Which replicas the R local slots of a CTA hold, and who runs the exchange.
+
+// Cluster layout: the G = nbeta/R CTAs of a cluster run one sequence; slot r
+// of cluster rank k is temperature k*R + r; the exchange runs on rank 0 over
+// distributed shared memory.
+template <int R>
+struct ClusterLayout {
+  static constexpr bool kSpread = false;
+  int rank, seq;
+  __device__ __forceinline__ int nact() const { return R; }
+  __device__ __forceinline__ int ibeta(int r) const { return rank * R + r; }
+  __device__ __forceinline__ int iseq(int) const { return seq; }
+  __device__ __forceinline__ bool owner() const { return rank == 0; }
+  __device__ __forceinline__ int own_seq() const { return seq; }
+  __device__ __forceinline__ int own_slot() const { return 0; }
+  __device__ __forceinline__ int ph_region(int nbeta) const { return seq * nbeta + rank * R; }
+};
+
+// Spread layout: the N CTAs of a cooperative launch (all resident at once)
+// share the nbeta*nseq replicas evenly, sequence-major (replica f = iseq*nbeta
+// + ibeta): CTA b holds f in [start, start + cnt) with cnt = nrep/N or one
+// more (spread_range), so that no SM holds more than ceil(N/SMs) CTAs' worth,
+// whatever nseq is (64 x 32 replicas on 152 SMs: 293 CTAs of 6-7 replicas
+// instead of 256 clusters' CTAs of 8 on some SMs and 0 on others).  With
+// R <= nbeta a CTA spans at most two sequences and holds at most one
+// sequence's ibeta = 0 replica, whose generator draws that sequence's
+// exchange; that CTA (the owner) runs the exchange through global memory.
+struct SpreadLayout {
+  static constexpr bool kSpread = true;
+  int start, cnt, nbeta;
+  int seq_lo, seq_hi;   // sequences held (seq_hi is seq_lo or seq_lo + 1)
+  int own, own_r;       // owned sequence (or -1) and the local slot of its ibeta 0
+  int own_ncta;         // CTAs holding replicas of the owned sequence
+  __device__ __forceinline__ int nact() const { return cnt; }
+  __device__ __forceinline__ int ibeta(int r) const { return (start + r) % nbeta; }
+  __device__ __forceinline__ int iseq(int r) const { return (start + r) / nbeta; }
+  __device__ __forceinline__ bool owner() const { return own >= 0; }
+  __device__ __forceinline__ int own_seq() const { return own; }
+  __device__ __forceinline__ int own_slot() const { return own_r; }
+  __device__ __forceinline__ int ph_region(int) const { return 0; }   // shared phases only
+};
+
+// Waits until *flag >= target (acquire).  Bounded: after kSpinLimit polls
+// (about a second) it sets the abort flag and CMC_ERR_TIMEOUT and returns
+// false; it also returns false as soon as another CTA has aborted.
+constexpr unsigned kSpinLimit = 1u << 20;
+__device__ __forceinline__ bool spin_until_geq(int *flag, int target, int *abort, int *status)
 {
-  const int rank = (int)cluster.block_rank();
+  cuda::atomic_ref<int, cuda::thread_scope_device> f(*flag), a(*abort);
+  unsigned ns = 32;
+  for (unsigned n = 0; n < kSpinLimit; ++n) {
+    if (f.load(cuda::memory_order_acquire) >= target) return true;
+    if (a.load(cuda::memory_order_relaxed) != 0) return false;
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
+  }
+  a.store(1, cuda::memory_order_relaxed);
+  set_status(status, CMC_ERR_TIMEOUT);
+  return false;
+}
+
+// replica_exchange (src/gpu_mcmc.cu:533-626) for nbeta <= 32 on warp 0 of
+// the exchange owner: slot s on lane s, chi^2 (`chi`, each lane's on entry),
+// tcur, owner and n_exch in registers, swaps by shuffles.  Every lane runs a
+// copy of the ibeta = 0 replica's generator (held by thread `own_slot`; the
+// same draws), so k and u are known warp-wide and the attempt loop has no
+// shared-memory round trips; that thread keeps the advanced generator.  The
+// results go to x_chi2 / x_tcur / x_perm / x_nexch.
+__device__ __forceinline__ void warp_exchange(float chi, bool burn, Rng &rng, int own_slot,
+                                              int nbeta, const float *x_beta, float *x_chi2,
+                                              int *x_tcur, int *x_perm, int *x_nexch,
+                                              int *status)
+{
+  const int lane = threadIdx.x & 31;
+  const bool slot = lane < nbeta;
+  const float bt = slot ? x_beta[lane] : 0.0f;
+  int tc = slot ? x_tcur[lane] : 0, own = lane, nx = slot ? x_nexch[lane] : 0;
+  Rng xr = warp_broadcast(rng, own_slot);
+  const int nb1 = nbeta - 1;
+  for (int ib = 0; ib < nbeta; ++ib) {
+    const int k = xr.index(nb1, status);
+    const float ck = __shfl_sync(0xffffffffu, chi, k);
+    const float ck1 = __shfl_sync(0xffffffffu, chi, k + 1);
+    const float bk = __shfl_sync(0xffffffffu, bt, k);
+    const float bk1 = __shfl_sync(0xffffffffu, bt, k + 1);
+    const int tk = __shfl_sync(0xffffffffu, tc, k), tk1 = __shfl_sync(0xffffffffu, tc, k + 1);
+    const int ok = __shfl_sync(0xffffffffu, own, k), ok1 = __shfl_sync(0xffffffffu, own, k + 1);
+    const float a = expf(-0.5f * (bk1 - bk) * (ck - ck1));
+    const float alpha = (a < 1.0f) ? a : 1.0f;
+    const float u = xr.uniform();
+    if (u <= alpha) {
+      if (lane == k) {
+        chi = ck1; tc = tk1; own = ok1;
+        if (!burn) nx += 1;
+      } else if (lane == k + 1) {
+        chi = ck; tc = tk; own = ok;
+      }
+    }
+  }
+  if (lane == own_slot) rng = xr;
+  if (slot) {
+    x_chi2[lane] = chi;
+    x_tcur[lane] = tc;
+    x_perm[lane] = own;
+    x_nexch[lane] = nx;
+  }
+}
+
+// The replicas of layout `lay` on the calling CTA (in the cluster layout, all
+// CTAs of the cluster call this with the same sequence).  `smem` is the CTA's
+// dynamic shared memory, at least make_plan(...).total bytes for this job;
+// `ctl` is used by the spread layout only.
+template <class Model, int R, class Lay>
+__device__ void run_replicas(const cmc_job &job, const typename Model::Packed &pk, const Lay &lay,
+                             const SpreadCtl &ctl, unsigned char *smem)
+{
   const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
   const int nbeta = job.nbeta, nseq = job.nseq, nptot = job.nptot, nprm = job.nprm;
   const int nadj = job.nadj;
+  const int nact = lay.nact();
 
   const SmemPlan P = make_plan(R, T, nptot, nprm, nbeta, nadj, sizeof(typename Model::Consts),
                                Model::scratch_bytes(pk, R));
@@ -48,15 +160,16 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   float *s_pmax = s_pmin + nptot;
   typename Model::Consts *s_consts = (typename Model::Consts *)(smem + P.consts);
   float *s_red = (float *)(smem + P.red);       // [R][NW]
-  float *x_chi2 = (float *)(smem + P.xch);      // rank 0: [nbeta] each
+  float *x_chi2 = (float *)(smem + P.xch);      // exchange owner: [nbeta] each
   int *x_perm = (int *)(x_chi2 + nbeta);
   int *x_tcur = x_perm + nbeta;
   int *x_nexch = x_tcur + nbeta;
   float *x_beta = (float *)(x_nexch + nbeta);
   float *st_p = (float *)(smem + P.stage);      // [R][nprm][kCH]
-  int *st_t = (int *)(st_p + R * nprm * kCH);   // [nbeta][kCH] (rank 0)
-  float *st_c = (float *)(st_t + nbeta * kCH);  // [kCH] (rank 0)
+  int *st_t = (int *)(st_p + R * nprm * kCH);   // [nbeta][kCH] (exchange owner)
+  float *st_c = (float *)(st_t + nbeta * kCH);  // [kCH] (exchange owner)
   float *scratch = (float *)(smem + P.scratch);
+  __shared__ int s_ok;
 
   Cta<Model, R> cta;
   cta.job = &job;
@@ -67,10 +180,11 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   cta.tid = tid;
   cta.nthreads = T;
 #pragma unroll
-  for (int r = 0; r < R; ++r) cta.ist[r] = (rank * R + r) * nseq + iseq;
-  cta.ph_region = iseq * nbeta + rank * R;
+  for (int r = 0; r < R; ++r) cta.ist[r] = (r < nact) ? lay.ibeta(r) * nseq + lay.iseq(r) : 0;
+  cta.ph_region = lay.ph_region(nbeta);
 
-  // ---- load tables and state -------------------------------------------
+  // ---- load tables and state (slots r >= nact, spread layout only, stay
+  //      empty: flag 0, never proposed, evaluated on zero constants) --------
   for (int i = tid; i < nprm; i += T) s_ivar[i] = job.ivar[i];
   for (int i = tid; i < nptot; i += T) {
     s_pdescr[i] = job.pdescr[i];
@@ -79,33 +193,47 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   }
   for (int i = tid; i < R * nptot; i += T) {
     int r = i / nptot, j = i - r * nptot;
-    int ist = (rank * R + r) * nseq + iseq;
-    params[i] = job.pcur[(size_t)ist * nptot + j];
-    plast[i] = params[i];
+    float v = 0.0f;
+    if (r < nact) {
+      const int ist = lay.ibeta(r) * nseq + lay.iseq(r);
+      v = job.pcur[(size_t)ist * nptot + j];
+    }
+    params[i] = v;
+    plast[i] = v;
   }
   for (int i = tid; i < R * nprm; i += T) {
-    int r = i / nprm, k = i - r * nprm, ibeta = rank * R + r;
-    size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
-    s_pstp[i] = job.pstp[gi];
-    s_ncnt[i] = job.n_cnt[gi];
-    s_nacpt[i] = job.n_acpt[gi];
-    // n_hist[a][k][ibeta][iseq] for a = 0..nadj-1 -> one bit each; a ring
-    // holding other values than 0/1 keeps using the global array
+    int r = i / nprm, k = i - r * nprm;
     int h = 0, slow = 0;
-    for (int w = 0; w < HW; ++w) {
-      unsigned bits = 0u;
-      for (int b = 0; b < 32 && 32 * w + b < nadj; ++b) {
-        const int v = job.n_hist[(((size_t)nprm * (32 * w + b) + k) * nbeta + ibeta) * nseq + iseq];
-        h += v;
-        slow |= (v != 0 && v != 1);
-        bits |= (v != 0 ? 1u : 0u) << b;
+    if (r < nact) {
+      const int ibeta = lay.ibeta(r), iseq = lay.iseq(r);
+      size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
+      s_pstp[i] = job.pstp[gi];
+      s_ncnt[i] = job.n_cnt[gi];
+      s_nacpt[i] = job.n_acpt[gi];
+      // n_hist[a][k][ibeta][iseq] for a = 0..nadj-1 -> one bit each; a ring
+      // holding other values than 0/1 keeps using the global array
+      for (int w = 0; w < HW; ++w) {
+        unsigned bits = 0u;
+        for (int b = 0; b < 32 && 32 * w + b < nadj; ++b) {
+          const int v =
+              job.n_hist[(((size_t)nprm * (32 * w + b) + k) * nbeta + ibeta) * nseq + iseq];
+          h += v;
+          slow |= (v != 0 && v != 1);
+          bits |= (v != 0 ? 1u : 0u) << b;
+        }
+        s_hbits[i * HW + w] = bits;
       }
-      s_hbits[i * HW + w] = bits;
+    } else {
+      s_pstp[i] = 0.0f;
+      s_ncnt[i] = 0;
+      s_nacpt[i] = 0;
+      for (int w = 0; w < HW; ++w) s_hbits[i * HW + w] = 0u;
     }
     s_hsum[i] = h;
     s_hslow[i] = slow;
   }
-  if (rank == 0) {
+  if (lay.owner()) {
+    const int iseq = lay.own_seq();
     for (int s = tid; s < nbeta; s += T) {
       x_tcur[s] = job.tcur[s * nseq + iseq];
       x_nexch[s] = job.n_exch[s * nseq + iseq];
@@ -119,14 +247,22 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   rng.u = rng.n = nullptr;
   rng.cu = rng.cn = rng.lu = rng.ln = 0;
   if (tid < R) {
-    const int r = tid, ibeta = rank * R + r, ist = ibeta * nseq + iseq;
+    const int r = tid;
+    s_k[r] = 0;
+    s_evald[r] = 0;
+    s_flag[r] = 0;
+    s_chi2c[r] = 0.0f;
+    s_ptent[r] = 0.0f;
+    s_ptentn[r] = 0;
+    s_beta[r] = 0.0f;
+  }
+  if (tid < nact) {
+    const int r = tid, ibeta = lay.ibeta(r), iseq = lay.iseq(r), ist = ibeta * nseq + iseq;
     s_ptent[r] = job.ptent[ist];
     s_chi2c[r] = job.chi2c[ist];
     s_beta[r] = job.beta[ibeta];
     s_ptentn[r] = job.ptentn[ist];
     s_flag[r] = job.flag[ist];
-    s_k[r] = 0;
-    s_evald[r] = 0;
     if (rng.inj) {
       rng.u = job.inj_u + (size_t)ist * job.inj_lu;
       rng.n = job.inj_n + (size_t)ist * job.inj_ln;
@@ -150,7 +286,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
 
   // ---- init_pcur + first chi^2 (src/gpu_mcmc.cu:245-267, 714-719) ---------
   if (job.do_init) {
-    if (tid < R) {
+    if (tid < nact) {
       const int r = tid;
       s_flag[r] = 1;
       for (int i = 0; i < nprm; ++i) {
@@ -169,7 +305,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
     Model::template eval<R>(cta, acc);
     block_reduce<Model, R>(acc, s_red, tid, NW);
     __syncthreads();
-    if (tid < R) {
+    if (tid < nact) {
       float s = 0.f;
       for (int w = 0; w < NW; ++w) s += s_red[tid * NW + w];
       s_chi2c[tid] = s;
@@ -182,7 +318,6 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   // Runs on thread r, fused with that thread's next proposal so that one
   // barrier per proposal disappears.
   auto accept_adjust = [&](int r, bool burn) {
-    const int ibeta = rank * R + r;
     const int k = s_k[r];
     if (s_flag[r] != 0) {
       float c2 = 0.f;
@@ -209,7 +344,8 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
       if (modn < 0) modn += nadj;   // guards a negative n_cnt from the caller
       const int nw = (s_flag[r] != 0) ? 1 : 0;
       if (s_hslow[ik]) {
-        int *hp = &job.n_hist[(((size_t)nprm * modn + k) * nbeta + ibeta) * nseq + iseq];
+        int *hp = &job.n_hist[(((size_t)nprm * modn + k) * nbeta + lay.ibeta(r)) * nseq +
+                              lay.iseq(r)];
         s_hsum[ik] += nw - *hp;
         *hp = nw;
       } else {
@@ -233,7 +369,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   // prior box is rejected without evaluation (as in gen_proposal); the
   // pre-proposal parameters stay in blk for the rejection path.
   auto block_proposal = [&](int r) {
-    const float *L = job.prop_chol + (size_t)iseq * nprm * nprm;
+    const float *L = job.prop_chol + (size_t)lay.iseq(r) * nprm * nprm;
     float *acc = ptmp + r * nptot;
     for (int j = 0; j < nptot; ++j) blk[r * nptot + j] = params[r * nptot + j];
     for (int i = 0; i < nprm; ++i) acc[i] = 0.0f;
@@ -268,7 +404,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   for (int step = 0; step < nsteps; ++step) {
     const bool burn = step < job.nburn;
     for (int ipm = 0; ipm < nprm; ++ipm) {
-      if (tid < R) {
+      if (tid < nact) {
         const int r = tid;
         if (ipm > 0) accept_adjust(r, burn);
         if (block) {
@@ -303,95 +439,123 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
       block_reduce<Model, R>(acc, s_red, tid, NW);
       __syncthreads();
     }
-    if (tid < R) accept_adjust(tid, burn);
+    if (tid < nact) accept_adjust(tid, burn);
 
     // ---- replica_exchange (src/gpu_mcmc.cu:533-626) ------------------------
     // nbeta attempts in the reference's order, drawn from the ibeta = 0
-    // replica's generator (thread 0 of cluster rank 0).
-    cluster.sync();
-    if (nbeta <= 32) {
-      // Warp 0 of rank 0, slot s on lane s: chi^2, tcur, owner and n_exch in
-      // registers, swaps by shuffles.  Every lane runs a copy of thread 0's
-      // generator (the same draws), so k and u are known warp-wide and the
-      // attempt loop has no shared-memory round trips; lane 0 keeps the
-      // advanced generator.
-      if (rank == 0 && tid < 32) {
-        const int lane = tid;
-        const bool slot = lane < nbeta;
-        float chi = slot ? cluster.map_shared_rank(s_chi2c, lane / R)[lane % R] : 0.0f;
-        const float bt = slot ? x_beta[lane] : 0.0f;
-        int tc = slot ? x_tcur[lane] : 0, own = lane, nx = slot ? x_nexch[lane] : 0;
-        Rng xr = warp_broadcast(rng, 0);
-        const int nb1 = nbeta - 1;
-        for (int ib = 0; ib < nbeta; ++ib) {
-          const int k = xr.index(nb1, job.status);
-          const float ck = __shfl_sync(0xffffffffu, chi, k);
-          const float ck1 = __shfl_sync(0xffffffffu, chi, k + 1);
-          const float bk = __shfl_sync(0xffffffffu, bt, k);
-          const float bk1 = __shfl_sync(0xffffffffu, bt, k + 1);
-          const int tk = __shfl_sync(0xffffffffu, tc, k), tk1 = __shfl_sync(0xffffffffu, tc, k + 1);
-          const int ok = __shfl_sync(0xffffffffu, own, k), ok1 = __shfl_sync(0xffffffffu, own, k + 1);
-          const float a = expf(-0.5f * (bk1 - bk) * (ck - ck1));
-          const float alpha = (a < 1.0f) ? a : 1.0f;
-          const float u = xr.uniform();
-          if (u <= alpha) {
-            if (lane == k) {
-              chi = ck1; tc = tk1; own = ok1;
-              if (!burn) nx += 1;
-            } else if (lane == k + 1) {
-              chi = ck; tc = tk; own = ok;
+    // replica's generator.
+    if constexpr (!Lay::kSpread) {
+      cg::cluster_group cluster = cg::this_cluster();
+      const int rank = lay.rank;
+      cluster.sync();
+      if (nbeta <= 32) {
+        if (rank == 0 && tid < 32) {
+          const float chi =
+              (tid < nbeta) ? cluster.map_shared_rank(s_chi2c, tid / R)[tid % R] : 0.0f;
+          warp_exchange(chi, burn, rng, 0, nbeta, x_beta, x_chi2, x_tcur, x_perm, x_nexch,
+                        job.status);
+        }
+      } else {
+        if (rank == 0) {
+          // gather the nbeta chi^2 values in parallel (one remote load each)
+          for (int s = tid; s < nbeta; s += T) {
+            x_chi2[s] = cluster.map_shared_rank(s_chi2c, s / R)[s % R];
+            x_perm[s] = s;
+          }
+          __syncthreads();
+        }
+        if (rank == 0 && tid == 0) {
+          const int nb1 = nbeta - 1;
+          for (int ib = 0; ib < nbeta; ++ib) {
+            const int k = rng.index(nb1, job.status);
+            const float a =
+                expf(-0.5f * (x_beta[k + 1] - x_beta[k]) * (x_chi2[k] - x_chi2[k + 1]));
+            const float alpha = (a < 1.0f) ? a : 1.0f;
+            const float u = rng.uniform();
+            if (u <= alpha) {
+              int ti = x_tcur[k]; x_tcur[k] = x_tcur[k + 1]; x_tcur[k + 1] = ti;
+              int pi = x_perm[k]; x_perm[k] = x_perm[k + 1]; x_perm[k + 1] = pi;
+              float cc = x_chi2[k]; x_chi2[k] = x_chi2[k + 1]; x_chi2[k + 1] = cc;
+              if (!burn) x_nexch[k] += 1;
             }
           }
         }
-        if (lane == 0) rng = xr;
-        if (slot) {
-          x_chi2[lane] = chi;
-          x_tcur[lane] = tc;
-          x_perm[lane] = own;
-          x_nexch[lane] = nx;
-        }
       }
+      cluster.sync();
+      {
+        const int *perm0 = cluster.map_shared_rank(x_perm, 0);
+        const float *chi0 = cluster.map_shared_rank(x_chi2, 0);
+        for (int i = tid; i < R * nptot; i += T) {
+          int r = i / nptot, j = i - r * nptot;
+          int src = perm0[rank * R + r];
+          const float *rp = cluster.map_shared_rank(params, src / R);
+          ptmp[i] = rp[(src % R) * nptot + j];
+        }
+        if (tid < R) ptmp[R * nptot + tid] = chi0[rank * R + tid];
+      }
+      cluster.sync();
+      for (int i = tid; i < R * nptot; i += T) params[i] = ptmp[i];
+      if (tid < R) s_chi2c[tid] = ptmp[R * nptot + tid];
+      __syncthreads();
     } else {
-      if (rank == 0) {
-        // gather the nbeta chi^2 values in parallel (one remote load each)
-        for (int s = tid; s < nbeta; s += T) {
-          x_chi2[s] = cluster.map_shared_rank(s_chi2c, s / R)[s % R];
-          x_perm[s] = s;
-        }
-        __syncthreads();
+      // Publish this CTA's replicas, count in at their sequences, let each
+      // sequence's owner run the exchange, and pull the new rows.  The waits
+      // are bounded (spin_until_geq); after an abort every CTA leaves the
+      // iteration loop and writes its state back with the error status set.
+      using AtomicInt = cuda::atomic_ref<int, cuda::thread_scope_device>;
+      const size_t nrep = (size_t)nbeta * nseq, par = (size_t)(step & 1);
+      float *xp = ctl.xp + par * nrep * nptot;
+      float *xc = ctl.xc + par * nrep;
+      int *xperm = ctl.xperm + par * nrep;
+      float *xchi = ctl.xchi + par * nrep;
+      __syncthreads();   // the last accept_adjust may have restored a row
+      for (int i = tid; i < nact * nptot; i += T) xp[(size_t)lay.start * nptot + i] = params[i];
+      if (tid < nact) xc[lay.start + tid] = s_chi2c[tid];
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) {
+        __threadfence();
+        for (int s = lay.seq_lo; s <= lay.seq_hi; ++s)
+          AtomicInt(ctl.arrive[s]).fetch_add(1, cuda::memory_order_release);
       }
-      if (rank == 0 && tid == 0) {
-        const int nb1 = nbeta - 1;
-        for (int ib = 0; ib < nbeta; ++ib) {
-          const int k = rng.index(nb1, job.status);
-          const float a = expf(-0.5f * (x_beta[k + 1] - x_beta[k]) * (x_chi2[k] - x_chi2[k + 1]));
-          const float alpha = (a < 1.0f) ? a : 1.0f;
-          const float u = rng.uniform();
-          if (u <= alpha) {
-            int ti = x_tcur[k]; x_tcur[k] = x_tcur[k + 1]; x_tcur[k + 1] = ti;
-            int pi = x_perm[k]; x_perm[k] = x_perm[k + 1]; x_perm[k + 1] = pi;
-            float cc = x_chi2[k]; x_chi2[k] = x_chi2[k + 1]; x_chi2[k + 1] = cc;
-            if (!burn) x_nexch[k] += 1;
+      if (lay.owner() && tid < 32) {
+        const int s = lay.own_seq();
+        int ok = 1;
+        if (tid == 0) {
+          ok = spin_until_geq(&ctl.arrive[s], (step + 1) * lay.own_ncta, ctl.abort, job.status);
+          __threadfence();
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (ok) {
+          const float chi = (tid < nbeta) ? __ldcg(&xc[(size_t)s * nbeta + tid]) : 0.0f;
+          warp_exchange(chi, burn, rng, lay.own_slot(), nbeta, x_beta, x_chi2, x_tcur, x_perm,
+                        x_nexch, job.status);
+          if (tid < nbeta) {
+            xperm[(size_t)s * nbeta + tid] = x_perm[tid];
+            xchi[(size_t)s * nbeta + tid] = x_chi2[tid];
           }
+          __threadfence();
+          __syncwarp();
+          if (tid == 0) AtomicInt(ctl.done[s]).store(step + 1, cuda::memory_order_release);
         }
       }
-    }
-    cluster.sync();
-    {
-      const int *perm0 = cluster.map_shared_rank(x_perm, 0);
-      const float *chi0 = cluster.map_shared_rank(x_chi2, 0);
-      for (int i = tid; i < R * nptot; i += T) {
-        int r = i / nptot, j = i - r * nptot;
-        int src = perm0[rank * R + r];
-        const float *rp = cluster.map_shared_rank(params, src / R);
-        ptmp[i] = rp[(src % R) * nptot + j];
+      if (tid == 0) {
+        int ok = 1;
+        for (int s = lay.seq_lo; s <= lay.seq_hi && ok; ++s)
+          ok = spin_until_geq(&ctl.done[s], step + 1, ctl.abort, job.status) ? 1 : 0;
+        __threadfence();
+        s_ok = ok;
       }
-      if (tid < R) ptmp[R * nptot + tid] = chi0[rank * R + tid];
+      __syncthreads();
+      if (!s_ok) break;
+      for (int i = tid; i < nact * nptot; i += T) {
+        const int r = i / nptot, j = i - r * nptot, f = lay.start + r;
+        const int src = __ldcg(&xperm[f]);
+        params[i] = __ldcg(&xp[((size_t)(f - f % nbeta) + src) * nptot + j]);
+      }
+      if (tid < nact) s_chi2c[tid] = __ldcg(&xchi[lay.start + tid]);
+      __syncthreads();
     }
-    cluster.sync();
-    for (int i = tid; i < R * nptot; i += T) params[i] = ptmp[i];
-    if (tid < R) s_chi2c[tid] = ptmp[R * nptot + tid];
-    __syncthreads();
     Model::after_exchange(cta);
 
     // ---- record pout / tout / chi2 (main stage) ---------------------------
@@ -402,7 +566,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
         int r = i / nprm, k = i - r * nprm;
         st_p[i * kCH + slot] = params[r * nptot + s_ivar[k]];
       }
-      if (rank == 0) {
+      if (lay.owner()) {
         for (int s = tid; s < nbeta; s += T) st_t[s * kCH + slot] = x_tcur[s];
         if (tid == 0) st_c[slot] = x_chi2[0];
       }
@@ -411,13 +575,14 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
         const int cnt = slot + 1;
         const size_t col0 = (size_t)job.itr0 + (m - slot);
         const size_t ntot = (size_t)job.niter_total;
-        for (int i = tid; i < R * nprm * cnt; i += T) {
+        for (int i = tid; i < nact * nprm * cnt; i += T) {
           int rk = i / cnt, c = i - rk * cnt;
-          int r = rk / nprm, k = rk - r * nprm, ibeta = rank * R + r;
-          job.pout[(((size_t)k * nbeta + ibeta) * nseq + iseq) * ntot + col0 + c] =
+          int r = rk / nprm, k = rk - r * nprm;
+          job.pout[(((size_t)k * nbeta + lay.ibeta(r)) * nseq + lay.iseq(r)) * ntot + col0 + c] =
               st_p[rk * kCH + c];
         }
-        if (rank == 0) {
+        if (lay.owner()) {
+          const int iseq = lay.own_seq();
           for (int i = tid; i < nbeta * cnt; i += T) {
             int s = i / cnt, c = i - s * cnt;
             job.tout[((size_t)s * nseq + iseq) * ntot + col0 + c] = st_t[s * kCH + c];
@@ -430,13 +595,13 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   }
 
   // ---- write the state back ------------------------------------------------
-  for (int i = tid; i < R * nptot; i += T) {
+  for (int i = tid; i < nact * nptot; i += T) {
     int r = i / nptot, j = i - r * nptot;
-    int ist = (rank * R + r) * nseq + iseq;
+    int ist = lay.ibeta(r) * nseq + lay.iseq(r);
     job.pcur[(size_t)ist * nptot + j] = params[i];
   }
-  for (int i = tid; i < R * nprm; i += T) {
-    int r = i / nprm, k = i - r * nprm, ibeta = rank * R + r;
+  for (int i = tid; i < nact * nprm; i += T) {
+    int r = i / nprm, k = i - r * nprm, ibeta = lay.ibeta(r), iseq = lay.iseq(r);
     size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
     job.pstp[gi] = s_pstp[i];
     job.n_cnt[gi] = s_ncnt[i];
@@ -447,14 +612,15 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
             (s_hbits[i * HW + (a >> 5)] >> (a & 31)) & 1u;
     }
   }
-  if (rank == 0) {
+  if (lay.owner()) {
+    const int iseq = lay.own_seq();
     for (int s = tid; s < nbeta; s += T) {
       job.tcur[s * nseq + iseq] = x_tcur[s];
       job.n_exch[s * nseq + iseq] = x_nexch[s];
     }
   }
-  if (tid < R) {
-    const int r = tid, ist = (rank * R + r) * nseq + iseq;
+  if (tid < nact) {
+    const int r = tid, ist = lay.ibeta(r) * nseq + lay.iseq(r);
     job.chi2c[ist] = s_chi2c[r];
     job.flag[ist] = s_flag[r];
     job.ptent[ist] = s_ptent[r];
@@ -471,7 +637,7 @@ __device__ void run_sequence(const cmc_job &job, const typename Model::Packed &p
   Model::template final_rows<R>(cta, plast, s_evald);
   // No CTA may leave (or start its next sequence) while another can still
   // read its shared memory.
-  cluster.sync();
+  if constexpr (!Lay::kSpread) cg::this_cluster().sync();
 }
 
 // One launch for one job: cluster c runs sequence c.  (The kernel bodies are
@@ -482,7 +648,10 @@ __device__ __forceinline__ void sweep_body(const cmc_job &job, const typename Mo
 {
   extern __shared__ __align__(16) unsigned char smem[];
   cg::cluster_group cluster = cg::this_cluster();
-  run_sequence<Model, R>(job, pk, blockIdx.x / (int)cluster.num_blocks(), cluster, smem);
+  ClusterLayout<R> lay;
+  lay.rank = (int)cluster.block_rank();
+  lay.seq = blockIdx.x / (int)cluster.num_blocks();
+  run_replicas<Model, R>(job, pk, lay, SpreadCtl{}, smem);
 }
 
 template <class Model, int R>
@@ -490,6 +659,42 @@ __global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
 sweep_kernel(const cmc_job job, const typename Model::Packed pk)
 {
   sweep_body<Model, R>(job, pk);
+}
+
+// One cooperative launch of N = gridDim.x CTAs in the spread layout.  The
+// host checks that the N CTAs are resident at once and that nbeta <= 32,
+// N <= nrep and ceil(nrep / N) <= R <= nbeta (every CTA's count fits its R
+// slots, and a CTA spans at most two sequences).
+template <class Model, int R>
+__device__ __forceinline__ void spread_body(const cmc_job &job, const typename Model::Packed &pk,
+                                            const SpreadCtl &ctl)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nbeta = job.nbeta, nrep = nbeta * job.nseq, N = (int)gridDim.x;
+  SpreadLayout lay;
+  lay.nbeta = nbeta;
+  spread_range(nrep, N, (int)blockIdx.x, lay.start, lay.cnt);
+  lay.seq_lo = lay.start / nbeta;
+  lay.seq_hi = (lay.start + lay.cnt - 1) / nbeta;
+  lay.own = -1;
+  lay.own_r = 0;
+  if (lay.start % nbeta == 0) {
+    lay.own = lay.seq_lo;
+  } else if (lay.seq_hi > lay.seq_lo) {
+    lay.own = lay.seq_hi;
+    lay.own_r = lay.seq_hi * nbeta - lay.start;
+  }
+  lay.own_ncta = 0;
+  if (lay.own >= 0)
+    lay.own_ncta = spread_cta_of(nrep, N, lay.own * nbeta + nbeta - 1) - (int)blockIdx.x + 1;
+  run_replicas<Model, R>(job, pk, lay, ctl, smem);
+}
+
+template <class Model, int R>
+__global__ void __launch_bounds__(kMaxThreads, CMC_MIN_BLOCKS)
+spread_kernel(const cmc_job job, const typename Model::Packed pk, const SpreadCtl ctl)
+{
+  spread_body<Model, R>(job, pk, ctl);
 }
 
 // Persistent launch over a work list of (job, sequence) items of many
@@ -531,7 +736,10 @@ __device__ __forceinline__ void batch_body(const cmc_job *jobs, const typename M
       s_job.itr0 = itr0;
     }
     __syncthreads();
-    run_sequence<Model, R>(s_job, s_pk, w.y, cluster, smem);
+    ClusterLayout<R> lay;
+    lay.rank = rank;
+    lay.seq = w.y;
+    run_replicas<Model, R>(s_job, s_pk, lay, SpreadCtl{}, smem);
   }
 }
 

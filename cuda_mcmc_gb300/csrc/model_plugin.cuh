@@ -25,6 +25,7 @@ struct PluginModel {
 
   static constexpr bool kRowsInEval = true;
   static constexpr int kMaxR = 32;  // instantiated replicas-per-CTA counts: 1 .. 32
+  static constexpr bool kSpread = false;   // cluster layout only
 
   // data points one replica's evaluation runs over
   __host__ __device__ static int points(const Packed &pk) { return pk.ndat * pk.npass; }

@@ -190,7 +190,11 @@ struct SgraModel {
   static constexpr int kGlobalPhaseMinPts = 2048;
 
   static constexpr bool kRowsInEval = false;
-  static constexpr int kMaxR = 8;   // instantiated replicas-per-CTA counts: 1, 2, 4, 8
+  // instantiated replicas-per-CTA counts: 1, 2, 4, 8 (cluster layout), 1..8
+  // (spread layout, phases in shared memory only: its one-short CTAs'
+  // unused slots write phases of their own)
+  static constexpr int kMaxR = 8;
+  static constexpr bool kSpread = true;
   static constexpr unsigned kTabBytes =
       (unsigned)sizeof(float4) * kBesselIntervals * ((kBesselDeg + 1) / 2);
 

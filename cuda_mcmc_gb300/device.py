@@ -162,7 +162,7 @@ class DeviceJob:
         j.work, j.work_bytes = _ptr(t["work"]), wb
         self.job = j
         self.itr_done = 0
-        self.shape = None          # forced launch shape {R, T, phasor} (see autotune.py)
+        self.shape = None          # forced launch shape {R, T, phasor[, layout]} (autotune.py)
 
     @classmethod
     def from_workload(cls, w, niter_total=None, seed=1234, rng="curand", streams=None,
@@ -190,13 +190,11 @@ class DeviceJob:
         j.nburn, j.niter = int(nburn), int(niter)
         j.itr0 = self.itr_done if itr0 is None else int(itr0)
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
-        if self.shape:
-            self.L.cmc_set_config(self.shape["R"], self.shape["T"], self.shape["phasor"])
+        self._force_shape()
         try:
             _lib.check(self.L, self.L.cmc_run(C.byref(j), C.c_void_p(s.cuda_stream)))
         finally:
-            if self.shape:
-                self.L.cmc_set_config(0, 0, -1)
+            self._release_shape()
         self.itr_done = j.itr0 + j.niter
 
     def graph_schedule(self, nburn, niter, chunk=256, itr0=0):
@@ -239,21 +237,33 @@ class DeviceJob:
         if st:
             raise _lib.McmcError(st, "device status %d (see cmc_status in cmc_job.h)" % st)
 
-    def config(self):
-        """Launch shape used for this job: (R, G, T, phasor, smem, clusters/wave)."""
-        R, G, T, P, W = (C.c_int() for _ in range(5))
-        sm = C.c_size_t()
+    def _force_shape(self):
         if self.shape:
             self.L.cmc_set_config(self.shape["R"], self.shape["T"], self.shape["phasor"])
+            self.L.cmc_set_layout(int(self.shape.get("layout", 0)))
+
+    def _release_shape(self):
+        if self.shape:
+            self.L.cmc_set_config(0, 0, -1)
+            self.L.cmc_set_layout(0)
+
+    def config(self):
+        """Launch shape used for this job: R, G, T, phasor, smem, clusters/wave
+        and the layout ("cluster", or "spread" with G = 0 and `blocks` CTAs)."""
+        R, G, T, P, W = (C.c_int() for _ in range(5))
+        sm = C.c_size_t()
+        self._force_shape()
         try:
             _lib.check(self.L, self.L.cmc_query_config(C.byref(self.job), C.byref(R), C.byref(G),
                                                        C.byref(T), C.byref(P), C.byref(sm),
                                                        C.byref(W)))
         finally:
-            if self.shape:
-                self.L.cmc_set_config(0, 0, -1)
-        return dict(R=R.value, G=G.value, T=T.value, phasor=P.value, smem=sm.value,
-                    clusters_per_wave=W.value)
+            self._release_shape()
+        out = dict(R=R.value, G=G.value, T=T.value, phasor=P.value, smem=sm.value,
+                   clusters_per_wave=W.value, layout="cluster" if G.value else "spread")
+        if not G.value:
+            out["blocks"] = W.value
+        return out
 
     # ---- state access ----------------------------------------------------------
     def to_numpy(self, fields=STATE_FIELDS):

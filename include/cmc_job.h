@@ -18,7 +18,9 @@ enum cmc_status {
   CMC_ERR_STREAM = 3,     /* an injected random stream ran out                */
   CMC_ERR_MODEL = 4,      /* the model reported an error (e.g. bad imodel)    */
   CMC_ERR_NOMEM = 5,      /* device allocation failed                         */
-  CMC_ERR_UNSUPPORTED = 6 /* no kernel configuration fits these sizes         */
+  CMC_ERR_UNSUPPORTED = 6, /* no kernel configuration fits these sizes        */
+  CMC_ERR_TIMEOUT = 7     /* a wait between the CTAs of a spread-layout sweep
+                             ran out (cmc_set_layout)                         */
 };
 
 enum cmc_prop_mode {

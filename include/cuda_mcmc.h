@@ -181,7 +181,8 @@ size_t cmc_work_bytes(const cmc_job *job, int mode);
  * CTA R, cluster size G = nbeta/R, threads per CTA T, closure storage
  * (1 = unit phasors, 0 = phases in shared memory, 2 = phases in global
  * memory, which needs job->work of cmc_work_bytes(job, 0) bytes), dynamic
- * shared memory and resident clusters per wave.  The reference always launches <<<nseq, nbeta>>> per
+ * shared memory and resident clusters per wave.  In the spread layout (see
+ * cmc_set_layout) G is 0 and *clusters_per_wave is the number of CTAs.  The reference always launches <<<nseq, nbeta>>> per
  * step kernel and <<<nbeta*nseq*ndat/128+1, 128>>> for the model
  * (src/gpu_mcmc.cu:686-687). */
 int cmc_query_config(const cmc_job *job, int *R, int *G, int *T, int *phasor, size_t *smem,
@@ -190,6 +191,17 @@ int cmc_query_config(const cmc_job *job, int *R, int *G, int *T, int *phasor, si
 /* Force a launch shape (0 / -1 = automatic), e.g. from the autotuner.  No
  * reference counterpart (the reference's shape is fixed). */
 void cmc_set_config(int R, int T, int phasor);
+
+/* Force the replica layout of cmc_run's sweep (0 = automatic).  1: one
+ * thread-block cluster per sequence, its nbeta/R CTAs holding R temperatures
+ * each, the exchange over distributed shared memory.  2 (built-in Sgr A*
+ * model, nbeta <= 32, job->work of cmc_work_bytes(job, 0) bytes): one
+ * cooperative launch whose CTAs share the nbeta*nseq replicas evenly (R or
+ * R - 1 each, sequence-major), each sequence's exchange run by the CTA
+ * holding its ibeta = 0 replica through job->work; the automatic choice
+ * takes it where it leaves fewer replicas on the busiest SM.  Same chains
+ * either way.  No reference counterpart. */
+void cmc_set_layout(int layout);
 
 /* libcmc_module.so only; no reference counterpart.  That library is the
  * plugin C-ABI without a model compiled in: its launches take the kernels

@@ -276,11 +276,17 @@ def test_sweep_lockstep_vs_fp64_oracle(cfg):
 #         the cluster;
 #   cfg4: the 20000-visibility shape, R = 4, T = 256, phases in global memory
 #         (3000 + 900 data: from 2048 points on the phases may live there);
-#   r2g16: R = 2, the largest (non-portable) cluster, G = 16, unit phasors.
+#   r2g16: R = 2, the largest (non-portable) cluster, G = 16, unit phasors;
+#   spread: the spread layout (cmc_set_layout 2), 64 replicas shared by
+#         cooperative CTAs of 7 (10 CTAs: 7 7 7 7 6 6 6 6 6 6, the fifth
+#         holding both sequences and running the second one's exchange) or of
+#         3 (22 CTAs), the exchanges through global memory.
 SHAPES = {
     "cfg3_R8_T256_smem": (dict(nvis=2000, ncph=600), dict(R=8, T=256, phasor=0)),
     "cfg4_R4_T256_global": (dict(nvis=3000, ncph=900), dict(R=4, T=256, phasor=2)),
     "r2_g16_phasors": (dict(nvis=2000, ncph=600), dict(R=2, T=64, phasor=1)),
+    "spread_R7_T256_smem": (dict(nvis=2000, ncph=600), dict(R=7, T=256, phasor=0, layout=2)),
+    "spread_R3_T128_phasors": (dict(nvis=2000, ncph=600), dict(R=3, T=128, phasor=1, layout=2)),
 }
 
 
@@ -293,7 +299,10 @@ def test_sweep_lockstep_benchmark_shapes(name):
     job = _injected_job(w, 4, shape=shape)
     cfg = job.config()
     assert (cfg["R"], cfg["T"], cfg["phasor"]) == (shape["R"], shape["T"], shape["phasor"])
-    assert cfg["G"] == 32 // shape["R"]
+    if shape.get("layout") == 2:
+        assert cfg["layout"] == "spread" and cfg["blocks"] == -(-64 // shape["R"])
+    else:
+        assert cfg["G"] == 32 // shape["R"]
     job.run(0, 0, do_init=True)
     job.check()
     _check_init(w, job)

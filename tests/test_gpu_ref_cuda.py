@@ -74,6 +74,9 @@ CASES = {
     "2000vis_2x32_R8_G4": (dict(nseq=2, nbeta=32), dict(R=8, T=256, phasor=0), 4, 4),
     # the library's own choice at 32 temperatures
     "2000vis_4x32": (dict(nseq=4, nbeta=32), None, 3, 3),
+    # the spread layout: 128 replicas in 19 cooperative CTAs of 6-7, CTAs
+    # spanning two sequences, the exchanges through global memory
+    "2000vis_4x32_spread_R7": (dict(nseq=4, nbeta=32), dict(R=7, T=256, phasor=0, layout=2), 3, 3),
 }
 
 
