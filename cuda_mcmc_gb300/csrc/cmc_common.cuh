@@ -191,6 +191,9 @@ struct SpreadCtl {
   float *xc;     // [2][nrep] chi^2 before the exchange
   int *xperm;    // [2][nrep] source temperature of each slot after the exchange
   float *xchi;   // [2][nrep] chi^2 after the exchange
+  int hold;      // test hook: the owner of this sequence never completes its
+                 // exchange, so that every wait runs out (-1: none; set from
+                 // the environment variable CMC_SPREAD_HOLD_SEQ)
 };
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -219,6 +222,7 @@ __host__ __device__ inline SpreadCtl spread_ctl_at(unsigned char *base, int nseq
   c.xc = reinterpret_cast<float *>(base + o);  o += align256(4 * 2 * nrep);
   c.xperm = reinterpret_cast<int *>(base + o); o += align256(4 * 2 * nrep);
   c.xchi = reinterpret_cast<float *>(base + o);
+  c.hold = -1;
   return c;
 }
 

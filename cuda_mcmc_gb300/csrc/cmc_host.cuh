@@ -164,8 +164,8 @@ inline size_t spread_offset(const typename Model::Packed &pk)
 }
 
 // The spread layout can run this job: the model has it, every sequence's
-// exchange fits one warp (nbeta <= 32), the phases stay in shared memory
-// (pk.phasor is decided by the caller) and job.work holds the exchange area.
+// exchange fits one warp (nbeta <= 32) and job.work holds the exchange area
+// (after the phase regions, of which the model allocates nrep + kMaxR).
 template <class Model>
 inline bool spread_ok(const cmc_job &j, const typename Model::Packed &pk)
 {
@@ -294,9 +294,11 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         if (Tfix && T != Tfix) continue;
         if (spread_auto && T != out.T) continue;
         if (T < 32 * ((R + 31) / 32)) continue;
-        for (int ph = 1; ph >= 0; --ph) {
+        for (int ph = 2; ph >= 0; --ph) {
           if (Pfix >= 0 && ph != Pfix) continue;
           if (spread_auto && ph != out.phasor) continue;
+          if (ph == 2 && (!global_phases_ok<Model>(pk) || N * R > j.nbeta * j.nseq + Model::kMaxR))
+            continue;
           typename Model::Packed q = pk;
           q.phasor = ph;
           if (!spread_ok<Model>(j, q)) continue;
@@ -311,7 +313,8 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
           if (spread_auto && (load >= load_c || per_sm < per_sm_c)) continue;
           const int tpr = T / R;
           const int shape_rank = (tpr >= 32 && tpr < 64) ? 0 : (tpr >= 16 && tpr < 128) ? 1 : 2;
-          const double score = load * 1000.0 + shape_rank * 100.0 + (ph == 1 ? 0 : 10) - R;
+          const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
+          const double score = load * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 - R;
           if (score < best_s - 1e-9) {
             best_s = score;
             bs = LaunchCfg{};
@@ -330,8 +333,8 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
     } else if (Lfix == 2) {
       return fail(CMC_ERR_UNSUPPORTED,
                   "no spread-layout launch shape fits: it needs the built-in Sgr A* model, "
-                  "nbeta <= 32, phases in shared memory, job.work of cmc_work_bytes() bytes "
-                  "and at most as many CTAs as are resident at once");
+                  "nbeta <= 32, job.work of cmc_work_bytes() bytes and at most as many CTAs "
+                  "as are resident at once");
     }
   }
   if (!found)

@@ -2,6 +2,7 @@
 // instance translation units only (inst_sgra.cu, inst_plugin.cu), each of
 // which instantiates one value of R for its model.
 #pragma once
+#include <cstdlib>
 #include <string>
 
 #include "cmc_eval.cuh"
@@ -167,7 +168,8 @@ int launch_spread(const cmc_job &j, const typename Model::Packed &pk, const Laun
   e = cudaMemsetAsync(ctl, 0, spread_ctl_counter_bytes(j.nseq), s);
   if (e != cudaSuccess)
     return fail(CMC_ERR_CUDA, std::string("spread counters: ") + cudaGetErrorString(e));
-  const SpreadCtl x = spread_ctl_at(static_cast<unsigned char *>(ctl), j.nseq, j.nbeta, j.nptot);
+  SpreadCtl x = spread_ctl_at(static_cast<unsigned char *>(ctl), j.nseq, j.nbeta, j.nptot);
+  if (const char *h = std::getenv("CMC_SPREAD_HOLD_SEQ")) x.hold = std::atoi(h);   // test hook
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

@@ -48,13 +48,14 @@ struct SpreadLayout {
   int seq_lo, seq_hi;   // sequences held (seq_hi is seq_lo or seq_lo + 1)
   int own, own_r;       // owned sequence (or -1) and the local slot of its ibeta 0
   int own_ncta;         // CTAs holding replicas of the owned sequence
+  int region0;          // first of the CTA's R global phase regions (block * R)
   __device__ __forceinline__ int nact() const { return cnt; }
   __device__ __forceinline__ int ibeta(int r) const { return (start + r) % nbeta; }
   __device__ __forceinline__ int iseq(int r) const { return (start + r) / nbeta; }
   __device__ __forceinline__ bool owner() const { return own >= 0; }
   __device__ __forceinline__ int own_seq() const { return own; }
   __device__ __forceinline__ int own_slot() const { return own_r; }
-  __device__ __forceinline__ int ph_region(int) const { return 0; }   // shared phases only
+  __device__ __forceinline__ int ph_region(int) const { return region0; }
 };
 
 // Waits until *flag >= target (acquire).  The first kSpinFast polls follow
@@ -538,7 +539,8 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
           }
           __threadfence();
           __syncwarp();
-          if (tid == 0) AtomicInt(ctl.done[s]).store(step + 1, cuda::memory_order_release);
+          if (tid == 0 && s != ctl.hold)
+            AtomicInt(ctl.done[s]).store(step + 1, cuda::memory_order_release);
         }
       }
       if (tid == 0) {
@@ -666,7 +668,8 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
 // One cooperative launch of N = gridDim.x CTAs in the spread layout.  The
 // host checks that the N CTAs are resident at once and that nbeta <= 32,
 // N <= nrep and ceil(nrep / N) <= R <= nbeta (every CTA's count fits its R
-// slots, and a CTA spans at most two sequences).
+// slots, and a CTA spans at most two sequences); with phases in global
+// memory, that the job's phase area holds N*R regions.
 template <class Model, int R>
 __device__ __forceinline__ void spread_body(const cmc_job &job, const typename Model::Packed &pk,
                                             const SpreadCtl &ctl)
@@ -686,6 +689,7 @@ __device__ __forceinline__ void spread_body(const cmc_job &job, const typename M
     lay.own = lay.seq_hi;
     lay.own_r = lay.seq_hi * nbeta - lay.start;
   }
+  lay.region0 = (int)blockIdx.x * R;
   lay.own_ncta = 0;
   if (lay.own >= 0)
     lay.own_ncta = spread_cta_of(nrep, N, lay.own * nbeta + nbeta - 1) - (int)blockIdx.x + 1;

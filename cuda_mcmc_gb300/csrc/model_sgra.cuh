@@ -191,8 +191,8 @@ struct SgraModel {
 
   static constexpr bool kRowsInEval = false;
   // instantiated replicas-per-CTA counts: 1, 2, 4, 8 (cluster layout), 1..8
-  // (spread layout, phases in shared memory only: its one-short CTAs'
-  // unused slots write phases of their own)
+  // (spread layout; a one-short CTA's unused slot writes phases of its own,
+  // in shared memory or in the CTA's own global region)
   static constexpr int kMaxR = 8;
   static constexpr bool kSpread = true;
   static constexpr unsigned kTabBytes =
@@ -277,11 +277,14 @@ struct SgraModel {
   }
 
   // packed data + the global phase regions when the data set is large enough
-  // to use them (cmc_work_bytes reports this size)
+  // to use them (cmc_work_bytes reports this size): one per replica, and
+  // kMaxR more for the spread layout, whose CTAs own R regions each
+  // (N*R <= nrep + R - 1)
   static size_t host_work_bytes(const Packed &pk)
   {
     size_t b = host_work_bytes_min(pk);
-    if (pk.npts >= kGlobalPhaseMinPts) b += (size_t)pk.nrep * pk.npts * sizeof(float);
+    if (pk.npts >= kGlobalPhaseMinPts)
+      b += ((size_t)pk.nrep + kMaxR) * pk.npts * sizeof(float);
     return b;
   }
 

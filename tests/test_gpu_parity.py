@@ -280,13 +280,15 @@ def test_sweep_lockstep_vs_fp64_oracle(cfg):
 #   spread: the spread layout (cmc_set_layout 2), 64 replicas shared by
 #         cooperative CTAs of 7 (10 CTAs: 7 7 7 7 6 6 6 6 6 6, the fifth
 #         holding both sequences and running the second one's exchange) or of
-#         3 (22 CTAs), the exchanges through global memory.
+#         3 (22 CTAs), the exchanges through global memory; with phases in
+#         global memory, one region per CTA slot.
 SHAPES = {
     "cfg3_R8_T256_smem": (dict(nvis=2000, ncph=600), dict(R=8, T=256, phasor=0)),
     "cfg4_R4_T256_global": (dict(nvis=3000, ncph=900), dict(R=4, T=256, phasor=2)),
     "r2_g16_phasors": (dict(nvis=2000, ncph=600), dict(R=2, T=64, phasor=1)),
     "spread_R7_T256_smem": (dict(nvis=2000, ncph=600), dict(R=7, T=256, phasor=0, layout=2)),
     "spread_R3_T128_phasors": (dict(nvis=2000, ncph=600), dict(R=3, T=128, phasor=1, layout=2)),
+    "spread_R7_T256_global": (dict(nvis=3000, ncph=900), dict(R=7, T=256, phasor=2, layout=2)),
 }
 
 

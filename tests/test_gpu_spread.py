@@ -136,17 +136,49 @@ def test_spread_is_the_automatic_choice_at_64x32():
     assert np.array_equal(datm, dev["datm"]) and np.array_equal(chi2m, dev["chi2m"])
 
 
+def test_spread_global_phases_equal_cluster_layout():
+    """Phases in global memory (3000 + 900 data): each spread CTA owns R
+    regions, so a one-short CTA's unused slot writes a region nobody reads;
+    the chains are the cluster layout's."""
+    w = synth.sgra(nvis=3000, ncph=900, seed=6, nseq=8, nbeta=32)
+    _, a = _run(w, dict(R=8, T=256, phasor=2, layout=1))
+    js, b = _run(w, dict(R=7, T=256, phasor=2, layout=2))
+    assert js.config()["phasor"] == 2
+    _same(a, b)
+
+
 def test_spread_rejects_what_it_cannot_run():
-    """Forced onto jobs it cannot hold (more than 32 temperatures; phases in
-    global memory), the spread layout reports no shape instead of running."""
+    """Forced onto a job it cannot hold (more than 32 temperatures), the
+    spread layout reports no shape instead of running."""
     from cuda_mcmc_gb300 import _lib
     w = synth.sgra(nvis=200, ncph=60, seed=8, nseq=1, nbeta=64)
     job = DeviceJob.from_workload(w, niter_total=1, seed=1)
     job.shape = dict(R=4, T=128, phasor=0, layout=2)
     with pytest.raises(_lib.McmcError):
         job.config()
-    w = synth.sgra(nvis=3000, ncph=900, seed=8, nseq=2, nbeta=32)
-    job = DeviceJob.from_workload(w, niter_total=1, seed=1)
-    job.shape = dict(R=4, T=256, phasor=2, layout=2)
-    with pytest.raises(_lib.McmcError):
-        job.config()
+
+
+def test_spread_wait_that_runs_out_reports_timeout(monkeypatch):
+    """A wait that nothing ends: with the test hook CMC_SPREAD_HOLD_SEQ the
+    owner of sequence 0 never completes its exchange.  Every CTA's bounded
+    wait runs out (about a second), the CTAs leave their iteration loops and
+    the launch ends with CMC_ERR_TIMEOUT in the status word; the context stays
+    usable and the next launch runs the normal chains."""
+    import time
+    from cuda_mcmc_gb300 import _lib
+    w = synth.sgra(nvis=400, ncph=120, seed=3, nseq=4, nbeta=16)
+    shape = dict(R=5, T=128, phasor=0, layout=2)
+    job = DeviceJob.from_workload(w, niter_total=2, seed=5)
+    job.shape = shape
+    monkeypatch.setenv("CMC_SPREAD_HOLD_SEQ", "0")
+    t0 = time.perf_counter()
+    job.run(2, 2, do_init=True)
+    with pytest.raises(_lib.McmcError) as err:
+        job.check()
+    elapsed = time.perf_counter() - t0
+    monkeypatch.delenv("CMC_SPREAD_HOLD_SEQ")
+    assert err.value.code == _lib.CMC_ERR_TIMEOUT
+    assert elapsed < 30.0
+    _, a = _run(w, dict(R=8, T=128, phasor=0, layout=1), nburn=2, niter=2)
+    _, b = _run(w, shape, nburn=2, niter=2)
+    _same(a, b)
