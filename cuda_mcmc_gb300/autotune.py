@@ -87,15 +87,15 @@ def candidates(job):
                     except _lib.McmcError:
                         continue
                     out.append(cfg)
-        # the spread layout (any R up to the model's largest, phases in
-        # shared memory; models without it report no shape)
+        # the spread layout (any R up to the model's largest; models without
+        # it report no shape)
         for R in range(1, 9):
             if R > job.nbeta:
                 continue
             for T in T_VALUES:
                 if T < 32 * ((R + 31) // 32):
                     continue
-                for ph in (1, 0):
+                for ph in (1, 0, 2):
                     L.cmc_set_config(R, T, ph)
                     L.cmc_set_layout(2)
                     try:
@@ -109,8 +109,11 @@ def candidates(job):
     return out
 
 
+_LAYOUTS = {"cluster": 1, "spread": 2}
+
+
 def _key(cfg):
-    return (cfg["R"], cfg["T"], cfg["phasor"], 2 if cfg.get("layout") == "spread" else 1)
+    return (cfg["R"], cfg["T"], cfg["phasor"], _LAYOUTS.get(cfg.get("layout"), 1))
 
 
 # a measured shape replaces the library's own pick only when it is faster

@@ -242,6 +242,7 @@ struct Cta {
   float model_f;                    // setup (read once per launch, held in registers)
 };
 
+
 template <class Model, int R>
 __device__ __forceinline__ void block_reduce(float (&acc)[R], float *red, int tid, int nw)
 {

@@ -1,4 +1,4 @@
-// cmc_sweep.cuh -- the fused MCMC-RE sweep kernel (one launch per run).
+// cmc_sweep.cuh -- the fused MCMC-RE sweep kernels (one launch per run).
 // The work decomposition and the reference functions it restates are
 // described at the top of cmc_common.cuh.
 #pragma once
@@ -24,39 +24,65 @@ template <int R>
 struct ClusterLayout {
   static constexpr bool kSpread = false;
   int rank, seq;
-  __device__ __forceinline__ int nact() const { return R; }
+  __device__ __forceinline__ bool active(int) const { return true; }
   __device__ __forceinline__ int ibeta(int r) const { return rank * R + r; }
   __device__ __forceinline__ int iseq(int) const { return seq; }
   __device__ __forceinline__ bool owner() const { return rank == 0; }
   __device__ __forceinline__ int own_seq() const { return seq; }
-  __device__ __forceinline__ int own_slot() const { return 0; }
   __device__ __forceinline__ int ph_region(int nbeta) const { return seq * nbeta + rank * R; }
 };
 
 // Spread layout: the N CTAs of a cooperative launch (all resident at once)
-// share the nbeta*nseq replicas evenly, sequence-major (replica f = iseq*nbeta
-// + ibeta): CTA b holds f in [start, start + cnt) with cnt = nrep/N or one
-// more (spread_range), so that no SM holds more than ceil(N/SMs) CTAs' worth,
-// whatever nseq is (64 x 32 replicas on 152 SMs: 293 CTAs of 6-7 replicas
-// instead of 256 clusters' CTAs of 8 on some SMs and 0 on others).  With
-// R <= nbeta a CTA spans at most two sequences and holds at most one
-// sequence's ibeta = 0 replica, whose generator draws that sequence's
-// exchange; that CTA (the owner) runs the exchange through global memory.
+// share the replicas evenly, sequence-major (replica f = iseq*nbeta +
+// ibeta): CTA b holds f in [gstart, gstart + cnt) with cnt = nrep/N or one
+// more (spread_range), so
+// that no SM holds more than ceil(N/SMs) CTAs' worth, whatever nseq is (64 x
+// 32 replicas on 152 SMs: 293 CTAs of 6-7 replicas instead of 256 clusters'
+// CTAs of 8 on some SMs and 0 on others).  With R <= nbeta a CTA spans at
+// most two sequences and holds at most one sequence's ibeta = 0 replica,
+// whose generator draws that sequence's exchange; that CTA (the owner) runs
+// the exchange through global memory.
 struct SpreadLayout {
   static constexpr bool kSpread = true;
-  int start, cnt, nbeta;
+  int gstart, cnt, nbeta;
   int seq_lo, seq_hi;   // sequences held (seq_hi is seq_lo or seq_lo + 1)
   int own, own_r;       // owned sequence (or -1) and the local slot of its ibeta 0
   int own_ncta;         // CTAs holding replicas of the owned sequence
-  int region0;          // first of the CTA's R global phase regions (block * R)
-  __device__ __forceinline__ int nact() const { return cnt; }
-  __device__ __forceinline__ int ibeta(int r) const { return (start + r) % nbeta; }
-  __device__ __forceinline__ int iseq(int r) const { return (start + r) / nbeta; }
+  int region0;          // first of the CTA's global phase regions
+  __device__ __forceinline__ bool active(int r) const { return r < cnt; }
+  __device__ __forceinline__ int ibeta(int r) const { return (gstart + r) % nbeta; }
+  __device__ __forceinline__ int iseq(int r) const { return (gstart + r) / nbeta; }
   __device__ __forceinline__ bool owner() const { return own >= 0; }
   __device__ __forceinline__ int own_seq() const { return own; }
   __device__ __forceinline__ int own_slot() const { return own_r; }
   __device__ __forceinline__ int ph_region(int) const { return region0; }
 };
+
+// CTA b of N spreading nseq sequences of nbeta replicas.
+__device__ __forceinline__ SpreadLayout make_spread_layout(int nbeta, int nseq, int N, int b,
+                                                           int region0)
+{
+  const int nrep = nbeta * nseq;
+  SpreadLayout lay;
+  int start = 0;
+  spread_range(nrep, N, b, start, lay.cnt);
+  lay.nbeta = nbeta;
+  lay.gstart = start;
+  lay.seq_lo = start / nbeta;
+  lay.seq_hi = (start + lay.cnt - 1) / nbeta;
+  lay.own = -1;
+  lay.own_r = 0;
+  if (start % nbeta == 0) {
+    lay.own = lay.seq_lo;
+  } else if (lay.seq_hi > lay.seq_lo) {
+    lay.own = lay.seq_hi;
+    lay.own_r = lay.seq_hi * nbeta - start;
+  }
+  lay.own_ncta = 0;
+  if (lay.own >= 0) lay.own_ncta = spread_cta_of(nrep, N, lay.own * nbeta + nbeta - 1) - b + 1;
+  lay.region0 = region0;
+  return lay;
+}
 
 // Waits until *flag >= target (acquire).  The first kSpinFast polls follow
 // each other directly (the waits of an exchange last microseconds; sleeping
@@ -126,131 +152,145 @@ __device__ __forceinline__ void warp_exchange(float chi, bool burn, Rng &rng, in
   }
 }
 
-// The replicas of layout `lay` on the calling CTA (in the cluster layout, all
-// CTAs of the cluster call this with the same sequence).  `smem` is the CTA's
-// dynamic shared memory, at least make_plan(...).total bytes for this job;
-// `ctl` is used by the spread layout only.
-template <class Model, int R, class Lay>
-__device__ void run_replicas(const cmc_job &job, const typename Model::Packed &pk, const Lay &lay,
-                             const SpreadCtl &ctl, unsigned char *smem)
-{
-  const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
-  const int nbeta = job.nbeta, nseq = job.nseq, nptot = job.nptot, nprm = job.nprm;
-  const int nadj = job.nadj;
-  const int nact = lay.nact();
+// ---- per-replica state of a CTA's R slots -------------------------------------
 
-  const SmemPlan P = make_plan(R, T, nptot, nprm, nbeta, nadj, sizeof(typename Model::Consts),
-                               Model::scratch_bytes(pk, R));
-  float *params = (float *)(smem + P.params);   // [R][nptot]
-  float *plast = (float *)(smem + P.plast);     // [R][nptot] params of last evaluation
-  float *ptmp = (float *)(smem + P.ptmp);       // [R][nptot] + [R] exchange staging
-  float *blk = (float *)(smem + P.blk);         // [R][nptot] block mode: pre-proposal params
-  const bool block = (job.prop_mode == CMC_PROP_BLOCK);
-  float *rf = (float *)(smem + P.rf);
-  int *ri = (int *)(smem + P.ri);
-  float *s_ptent = rf, *s_chi2c = rf + R, *s_chi2n = rf + 2 * R, *s_beta = rf + 3 * R;
-  int *s_ptentn = ri, *s_flag = ri + R, *s_k = ri + 2 * R, *s_evald = ri + 3 * R;
-  float *s_pstp = (float *)(smem + P.sf);       // [R][nprm]
-  int *s_ncnt = (int *)(smem + P.si);           // [R][nprm]
-  int *s_nacpt = s_ncnt + R * nprm;
-  int *s_hsum = s_nacpt + R * nprm;             // running sum of the history ring
-  int *s_hslow = s_hsum + R * nprm;             // 1: ring holds values other than 0/1
-  unsigned *s_hbits = (unsigned *)(smem + P.hist);   // [R][nprm][HW] history bits
-  const int HW = hist_words(nadj);
-  int *s_ivar = (int *)(smem + P.tab);
-  int *s_pdescr = s_ivar + nprm;
-  float *s_pmin = (float *)(s_pdescr + nptot);
-  float *s_pmax = s_pmin + nptot;
-  typename Model::Consts *s_consts = (typename Model::Consts *)(smem + P.consts);
-  float *s_red = (float *)(smem + P.red);       // [R][NW]
-  float *x_chi2 = (float *)(smem + P.xch);      // exchange owner: [nbeta] each
-  int *x_perm = (int *)(x_chi2 + nbeta);
-  int *x_tcur = x_perm + nbeta;
-  int *x_nexch = x_tcur + nbeta;
-  float *x_beta = (float *)(x_nexch + nbeta);
-  float *st_p = (float *)(smem + P.stage);      // [R][nprm][kCH]
-  int *st_t = (int *)(st_p + R * nprm * kCH);   // [nbeta][kCH] (exchange owner)
-  float *st_c = (float *)(st_t + nbeta * kCH);  // [kCH] (exchange owner)
-  float *scratch = (float *)(smem + P.scratch);
-  __shared__ int s_ok;
+// Shared-memory views of a sweep CTA (make_plan) and the steps of the
+// reference's per-replica kernels on one slot; slot r's steps run on the
+// thread holding slot r's generator.  Layouts give each slot's (ibeta, iseq)
+// and whether it is active (a spread CTA one replica short leaves its last
+// slot empty: flag 0, never proposed, evaluated on zero constants).
+template <class Model, int R>
+struct SweepState {
+  const cmc_job *job;
+  int nbeta, nseq, nptot, nprm, nadj, HW, NW;
+  bool block;
+  float *params, *plast, *ptmp, *blk;   // [R][nptot] each (ptmp: + [R])
+  float *s_ptent, *s_chi2c, *s_chi2n, *s_beta;
+  int *s_ptentn, *s_flag, *s_k, *s_evald;
+  float *s_pstp;                        // [R][nprm]
+  int *s_ncnt, *s_nacpt;                // [R][nprm]
+  int *s_hsum, *s_hslow;                // running history sum, 1: ring holds values other than 0/1
+  unsigned *s_hbits;                    // [R][nprm][HW] history bits
+  int *s_ivar, *s_pdescr;
+  float *s_pmin, *s_pmax;
+  typename Model::Consts *s_consts;     // [R]
+  float *s_red;                         // [R][NW] chi^2 partials of the last evaluation
+  float *x_chi2, *x_beta;               // exchange owner: [nbeta] each
+  int *x_perm, *x_tcur, *x_nexch;
+  float *st_p;                          // [R][nprm][kCH] staged pout rows
+  int *st_t;                            // [nbeta][kCH] staged tout (exchange owner)
+  float *st_c;                          // [kCH] staged chi2 (exchange owner)
+  float *scratch;                       // model scratch
 
-  Cta<Model, R> cta;
-  cta.job = &job;
-  cta.pk = &pk;
-  cta.consts = s_consts;
-  cta.flag = s_flag;
-  cta.scratch = scratch;
-  cta.tid = tid;
-  cta.nthreads = T;
-#pragma unroll
-  for (int r = 0; r < R; ++r) cta.ist[r] = (r < nact) ? lay.ibeta(r) * nseq + lay.iseq(r) : 0;
-  cta.ph_region = lay.ph_region(nbeta);
-
-  // ---- load tables and state (slots r >= nact, spread layout only, stay
-  //      empty: flag 0, never proposed, evaluated on zero constants) --------
-  for (int i = tid; i < nprm; i += T) s_ivar[i] = job.ivar[i];
-  for (int i = tid; i < nptot; i += T) {
-    s_pdescr[i] = job.pdescr[i];
-    s_pmin[i] = job.pmint[i];
-    s_pmax[i] = job.pmaxt[i];
+  __device__ void bind(const cmc_job &j, const SmemPlan &P, unsigned char *smem, int nw)
+  {
+    job = &j;
+    nbeta = j.nbeta; nseq = j.nseq; nptot = j.nptot; nprm = j.nprm; nadj = j.nadj;
+    HW = hist_words(nadj);
+    NW = nw;
+    block = (j.prop_mode == CMC_PROP_BLOCK);
+    params = (float *)(smem + P.params);
+    plast = (float *)(smem + P.plast);
+    ptmp = (float *)(smem + P.ptmp);
+    blk = (float *)(smem + P.blk);
+    float *rf = (float *)(smem + P.rf);
+    int *ri = (int *)(smem + P.ri);
+    s_ptent = rf; s_chi2c = rf + R; s_chi2n = rf + 2 * R; s_beta = rf + 3 * R;
+    s_ptentn = ri; s_flag = ri + R; s_k = ri + 2 * R; s_evald = ri + 3 * R;
+    s_pstp = (float *)(smem + P.sf);
+    s_ncnt = (int *)(smem + P.si);
+    s_nacpt = s_ncnt + R * nprm;
+    s_hsum = s_nacpt + R * nprm;
+    s_hslow = s_hsum + R * nprm;
+    s_hbits = (unsigned *)(smem + P.hist);
+    s_ivar = (int *)(smem + P.tab);
+    s_pdescr = s_ivar + nprm;
+    s_pmin = (float *)(s_pdescr + nptot);
+    s_pmax = s_pmin + nptot;
+    s_consts = (typename Model::Consts *)(smem + P.consts);
+    s_red = (float *)(smem + P.red);
+    x_chi2 = (float *)(smem + P.xch);
+    x_perm = (int *)(x_chi2 + nbeta);
+    x_tcur = x_perm + nbeta;
+    x_nexch = x_tcur + nbeta;
+    x_beta = (float *)(x_nexch + nbeta);
+    st_p = (float *)(smem + P.stage);
+    st_t = (int *)(st_p + R * nprm * kCH);
+    st_c = (float *)(st_t + nbeta * kCH);
+    scratch = (float *)(smem + P.scratch);
   }
-  for (int i = tid; i < R * nptot; i += T) {
-    int r = i / nptot, j = i - r * nptot;
-    float v = 0.0f;
-    if (r < nact) {
-      const int ist = lay.ibeta(r) * nseq + lay.iseq(r);
-      v = job.pcur[(size_t)ist * nptot + j];
+
+  // ---- loads (the CTA's threads tid of T) --------------------------------------
+  __device__ void load_tables(int tid, int T)
+  {
+    for (int i = tid; i < nprm; i += T) s_ivar[i] = job->ivar[i];
+    for (int i = tid; i < nptot; i += T) {
+      s_pdescr[i] = job->pdescr[i];
+      s_pmin[i] = job->pmint[i];
+      s_pmax[i] = job->pmaxt[i];
     }
-    params[i] = v;
-    plast[i] = v;
   }
-  for (int i = tid; i < R * nprm; i += T) {
-    int r = i / nprm, k = i - r * nprm;
-    int h = 0, slow = 0;
-    if (r < nact) {
-      const int ibeta = lay.ibeta(r), iseq = lay.iseq(r);
-      size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
-      s_pstp[i] = job.pstp[gi];
-      s_ncnt[i] = job.n_cnt[gi];
-      s_nacpt[i] = job.n_acpt[gi];
-      // n_hist[a][k][ibeta][iseq] for a = 0..nadj-1 -> one bit each; a ring
-      // holding other values than 0/1 keeps using the global array
-      for (int w = 0; w < HW; ++w) {
-        unsigned bits = 0u;
-        for (int b = 0; b < 32 && 32 * w + b < nadj; ++b) {
-          const int v =
-              job.n_hist[(((size_t)nprm * (32 * w + b) + k) * nbeta + ibeta) * nseq + iseq];
-          h += v;
-          slow |= (v != 0 && v != 1);
-          bits |= (v != 0 ? 1u : 0u) << b;
-        }
-        s_hbits[i * HW + w] = bits;
+  template <class Lay>
+  __device__ void load_rows(const Lay &lay, int tid, int T)
+  {
+    for (int i = tid; i < R * nptot; i += T) {
+      const int r = i / nptot, j = i - r * nptot;
+      float v = 0.0f;
+      if (lay.active(r)) {
+        const int ist = lay.ibeta(r) * nseq + lay.iseq(r);
+        v = job->pcur[(size_t)ist * nptot + j];
       }
-    } else {
-      s_pstp[i] = 0.0f;
-      s_ncnt[i] = 0;
-      s_nacpt[i] = 0;
-      for (int w = 0; w < HW; ++w) s_hbits[i * HW + w] = 0u;
+      params[i] = v;
+      plast[i] = v;
     }
-    s_hsum[i] = h;
-    s_hslow[i] = slow;
+    for (int i = tid; i < R * nprm; i += T) {
+      const int r = i / nprm, k = i - r * nprm;
+      int h = 0, slow = 0;
+      if (lay.active(r)) {
+        const int ibeta = lay.ibeta(r), iseq = lay.iseq(r);
+        const size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
+        s_pstp[i] = job->pstp[gi];
+        s_ncnt[i] = job->n_cnt[gi];
+        s_nacpt[i] = job->n_acpt[gi];
+        // n_hist[a][k][ibeta][iseq] for a = 0..nadj-1 -> one bit each; a ring
+        // holding other values than 0/1 keeps using the global array
+        for (int w = 0; w < HW; ++w) {
+          unsigned bits = 0u;
+          for (int b = 0; b < 32 && 32 * w + b < nadj; ++b) {
+            const int v =
+                job->n_hist[(((size_t)nprm * (32 * w + b) + k) * nbeta + ibeta) * nseq + iseq];
+            h += v;
+            slow |= (v != 0 && v != 1);
+            bits |= (v != 0 ? 1u : 0u) << b;
+          }
+          s_hbits[i * HW + w] = bits;
+        }
+      } else {
+        s_pstp[i] = 0.0f;
+        s_ncnt[i] = 0;
+        s_nacpt[i] = 0;
+        for (int w = 0; w < HW; ++w) s_hbits[i * HW + w] = 0u;
+      }
+      s_hsum[i] = h;
+      s_hslow[i] = slow;
+    }
   }
-  if (lay.owner()) {
-    const int iseq = lay.own_seq();
+  __device__ void load_exchange(int iseq, int tid, int T)
+  {
     for (int s = tid; s < nbeta; s += T) {
-      x_tcur[s] = job.tcur[s * nseq + iseq];
-      x_nexch[s] = job.n_exch[s * nseq + iseq];
-      x_beta[s] = job.beta[s];
+      x_tcur[s] = job->tcur[s * nseq + iseq];
+      x_nexch[s] = job->n_exch[s * nseq + iseq];
+      x_beta[s] = job->beta[s];
     }
   }
-
-  Rng rng;
-  rng.inj = (job.rng_mode == CMC_RNG_INJECTED);
-  rng.ovf = false;
-  rng.u = rng.n = nullptr;
-  rng.cu = rng.cn = rng.lu = rng.ln = 0;
-  if (tid < R) {
-    const int r = tid;
+  // slot r's scalars and generator (init_rng, src/gpu_mcmc.cu:228-239)
+  template <class Lay>
+  __device__ void load_slot(const Lay &lay, int r, Rng &rng)
+  {
+    rng.inj = (job->rng_mode == CMC_RNG_INJECTED);
+    rng.ovf = false;
+    rng.u = rng.n = nullptr;
+    rng.cu = rng.cn = rng.lu = rng.ln = 0;
     s_k[r] = 0;
     s_evald[r] = 0;
     s_flag[r] = 0;
@@ -258,73 +298,62 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
     s_ptent[r] = 0.0f;
     s_ptentn[r] = 0;
     s_beta[r] = 0.0f;
-  }
-  if (tid < nact) {
-    const int r = tid, ibeta = lay.ibeta(r), iseq = lay.iseq(r), ist = ibeta * nseq + iseq;
-    s_ptent[r] = job.ptent[ist];
-    s_chi2c[r] = job.chi2c[ist];
-    s_beta[r] = job.beta[ibeta];
-    s_ptentn[r] = job.ptentn[ist];
-    s_flag[r] = job.flag[ist];
+    if (!lay.active(r)) return;
+    const int ibeta = lay.ibeta(r), iseq = lay.iseq(r), ist = ibeta * nseq + iseq;
+    s_ptent[r] = job->ptent[ist];
+    s_chi2c[r] = job->chi2c[ist];
+    s_beta[r] = job->beta[ibeta];
+    s_ptentn[r] = job->ptentn[ist];
+    s_flag[r] = job->flag[ist];
     if (rng.inj) {
-      rng.u = job.inj_u + (size_t)ist * job.inj_lu;
-      rng.n = job.inj_n + (size_t)ist * job.inj_ln;
-      rng.lu = job.inj_lu;
-      rng.ln = job.inj_ln;
-      rng.cu = job.do_init ? 0 : job.inj_cur[2 * ist];
-      rng.cn = job.do_init ? 0 : job.inj_cur[2 * ist + 1];
-    } else if (job.do_init) {
+      rng.u = job->inj_u + (size_t)ist * job->inj_lu;
+      rng.n = job->inj_n + (size_t)ist * job->inj_ln;
+      rng.lu = job->inj_lu;
+      rng.ln = job->inj_ln;
+      rng.cu = job->do_init ? 0 : job->inj_cur[2 * ist];
+      rng.cn = job->do_init ? 0 : job->inj_cur[2 * ist + 1];
+    } else if (job->do_init) {
       // the replica's subsequence in the unsharded run (ist when unsharded)
       const unsigned long long sub =
-          job.nseq_total > 0
-              ? (unsigned long long)ibeta * job.nseq_total + job.seq_offset + iseq
+          job->nseq_total > 0
+              ? (unsigned long long)ibeta * job->nseq_total + job->seq_offset + iseq
               : (unsigned long long)ist;
-      curand_init(job.seed, sub, 0ull, &rng.st);
+      curand_init(job->seed, sub, 0ull, &rng.st);
     } else {
-      rng.st = reinterpret_cast<const curandStateXORWOW *>(job.rndst)[ist];
+      rng.st = reinterpret_cast<const curandStateXORWOW *>(job->rndst)[ist];
     }
   }
-  Model::setup(cta, tid, T);
-  __syncthreads();
 
-  // ---- init_pcur + first chi^2 (src/gpu_mcmc.cu:245-267, 714-719) ---------
-  if (job.do_init) {
-    if (tid < nact) {
-      const int r = tid;
-      s_flag[r] = 1;
-      for (int i = 0; i < nprm; ++i) {
-        int k = s_ivar[i];
-        float u = rng.uniform();
-        float p = __fmaf_rn(s_pmax[k] - s_pmin[k], u, s_pmin[k]);
-        if (s_pdescr[k] == 2) p = wrap_pi(p);
-        params[r * nptot + k] = p;
-      }
-      for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
-      Model::prepare(cta, r, &params[r * nptot]);
-      s_evald[r] = 1;
+  // ---- per-slot steps ------------------------------------------------------------
+  // init_pcur (src/gpu_mcmc.cu:245-267) and the constants of the first chi^2
+  template <class C>
+  __device__ void init_slot(int r, Rng &rng, C &cta)
+  {
+    s_flag[r] = 1;
+    for (int i = 0; i < nprm; ++i) {
+      const int k = s_ivar[i];
+      const float u = rng.uniform();
+      float p = __fmaf_rn(s_pmax[k] - s_pmin[k], u, s_pmin[k]);
+      if (s_pdescr[k] == 2) p = wrap_pi(p);
+      params[r * nptot + k] = p;
     }
-    __syncthreads();
-    float acc[R];
-    Model::template eval<R>(cta, acc);
-    block_reduce<Model, R>(acc, s_red, tid, NW);
-    __syncthreads();
-    if (tid < nact) {
-      float s = 0.f;
-      for (int w = 0; w < NW; ++w) s += s_red[tid * NW + w];
-      s_chi2c[tid] = s;
-    }
-    __syncthreads();
+    for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
+    Model::prepare(cta, r, &params[r * nptot]);
+    s_evald[r] = 1;
   }
-
+  __device__ float red_sum(int r) const
+  {
+    float s = 0.f;
+    for (int w = 0; w < NW; ++w) s += s_red[r * NW + w];
+    return s;
+  }
   // spmp_mcmc (src/gpu_mcmc.cu:426-474) and, in burn-in, adjust_steps
-  // (:480-526) for local replica r, after its proposal has been evaluated.
-  // Runs on thread r, fused with that thread's next proposal so that one
-  // barrier per proposal disappears.
-  auto accept_adjust = [&](int r, bool burn) {
+  // (:480-526) for slot r after its proposal has been evaluated.
+  __device__ void accept_adjust(int r, bool burn, int ibeta, int iseq, Rng &rng)
+  {
     const int k = s_k[r];
     if (s_flag[r] != 0) {
-      float c2 = 0.f;
-      for (int w = 0; w < NW; ++w) c2 += s_red[r * NW + w];
+      const float c2 = red_sum(r);
       s_chi2n[r] = c2;
       const float a = expf(-0.5f * s_beta[r] * (c2 - s_chi2c[r]));
       const float alpha = (a < 1.0f) ? a : 1.0f;
@@ -347,8 +376,7 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
       if (modn < 0) modn += nadj;   // guards a negative n_cnt from the caller
       const int nw = (s_flag[r] != 0) ? 1 : 0;
       if (s_hslow[ik]) {
-        int *hp = &job.n_hist[(((size_t)nprm * modn + k) * nbeta + lay.ibeta(r)) * nseq +
-                              lay.iseq(r)];
+        int *hp = &job->n_hist[(((size_t)nprm * modn + k) * nbeta + ibeta) * nseq + iseq];
         s_hsum[ik] += nw - *hp;
         *hp = nw;
       } else {
@@ -364,85 +392,301 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
         s_pstp[ik] = (float)((double)s_pstp[ik] * 1.01);
       s_ncnt[ik] = cnt + 1;
     }
-  };
-
-  // Block proposal for local replica r (thread r): all nprm parameters move,
-  // p_ivar[i] += pstp[0] * (L z)_i with z ~ N(0, I) drawn in order z_0..z_{nprm-1}
-  // and (L z)_i accumulated over j = 0..i by fmaf.  A proposal outside the
-  // prior box is rejected without evaluation (as in gen_proposal); the
-  // pre-proposal parameters stay in blk for the rejection path.
-  auto block_proposal = [&](int r) {
-    const float *L = job.prop_chol + (size_t)lay.iseq(r) * nprm * nprm;
-    float *acc = ptmp + r * nptot;
-    for (int j = 0; j < nptot; ++j) blk[r * nptot + j] = params[r * nptot + j];
-    for (int i = 0; i < nprm; ++i) acc[i] = 0.0f;
-    for (int j = 0; j < nprm; ++j) {
-      const float z = rng.normal();
-      for (int i = j; i < nprm; ++i) acc[i] = __fmaf_rn(__ldg(&L[i * nprm + j]), z, acc[i]);
-    }
-    const float sd = s_pstp[r * nprm];
-    bool out = false;
-    for (int i = 0; i < nprm; ++i) {
-      const int t = s_ivar[i];
-      float p = __fmaf_rn(sd, acc[i], blk[r * nptot + t]);
+  }
+  // gen_proposal (src/gpu_mcmc.cu:361-411) for slot r, or in block mode all
+  // nprm parameters at once, p_ivar[i] += pstp[0] * (L z)_i with z ~ N(0, I)
+  // drawn in order z_0..z_{nprm-1} and (L z)_i accumulated over j = 0..i by
+  // fmaf (the pre-proposal row kept in blk for the rejection path); then the
+  // model constants when the proposal is inside the prior box (a proposal
+  // outside is rejected without evaluation).
+  template <class C>
+  __device__ void propose(int r, int iseq, Rng &rng, C &cta)
+  {
+    if (block) {
+      const float *L = job->prop_chol + (size_t)iseq * nprm * nprm;
+      float *acc = ptmp + r * nptot;
+      for (int j = 0; j < nptot; ++j) blk[r * nptot + j] = params[r * nptot + j];
+      for (int i = 0; i < nprm; ++i) acc[i] = 0.0f;
+      for (int j = 0; j < nprm; ++j) {
+        const float z = rng.normal();
+        for (int i = j; i < nprm; ++i) acc[i] = __fmaf_rn(__ldg(&L[i * nprm + j]), z, acc[i]);
+      }
+      const float sd = s_pstp[r * nprm];
+      bool out = false;
+      for (int i = 0; i < nprm; ++i) {
+        const int t = s_ivar[i];
+        float p = __fmaf_rn(sd, acc[i], blk[r * nptot + t]);
+        if (s_pdescr[t] == 2) p = wrap_pi(p);
+        out |= (p < s_pmin[t]) || (p > s_pmax[t]);
+        params[r * nptot + t] = p;
+      }
+      s_k[r] = 0;
+      s_ptentn[r] = s_ivar[0];
+      s_ptent[r] = blk[r * nptot + s_ivar[0]];
+      if (out) {
+        for (int j = 0; j < nptot; ++j) params[r * nptot + j] = blk[r * nptot + j];
+        s_flag[r] = 0;
+        return;
+      }
+    } else {
+      const int k = rng.index(nprm, job->status);
+      const int t = s_ivar[k];
+      float p = params[r * nptot + t];
+      s_k[r] = k;
+      s_ptentn[r] = t;
+      s_ptent[r] = p;
+      const float sd = s_pstp[r * nprm + k];
+      const float rn = rng.normal();
+      p = __fmaf_rn(sd, rn, p);
       if (s_pdescr[t] == 2) p = wrap_pi(p);
-      out |= (p < s_pmin[t]) || (p > s_pmax[t]);
+      if ((p < s_pmin[t]) || (p > s_pmax[t])) {
+        s_flag[r] = 0;
+        return;
+      }
       params[r * nptot + t] = p;
     }
-    s_k[r] = 0;
-    s_ptentn[r] = s_ivar[0];
-    s_ptent[r] = blk[r * nptot + s_ivar[0]];
-    if (out) {
-      for (int j = 0; j < nptot; ++j) params[r * nptot + j] = blk[r * nptot + j];
-      s_flag[r] = 0;
-    } else {
-      s_flag[r] = 1;
-      for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
-      Model::prepare(cta, r, &params[r * nptot]);
-      s_evald[r] = 1;
-    }
-  };
+    s_flag[r] = 1;
+    for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
+    Model::prepare(cta, r, &params[r * nptot]);
+    s_evald[r] = 1;
+  }
 
+  // ---- records (pout / tout / chi2 of main iteration m) ----------------------------
+  // Every slot's row into staging column m % kCH.
+  __device__ void stage_rows(int slot, int tid, int T)
+  {
+    for (int i = tid; i < R * nprm; i += T) {
+      const int r = i / nprm, k = i - r * nprm;
+      st_p[i * kCH + slot] = params[r * nptot + s_ivar[k]];
+    }
+  }
+  // The staged columns [0, cnt) of the active slots to pout columns col0 ..
+  template <class Lay>
+  __device__ void flush_rows(const Lay &lay, int cnt, size_t col0, int tid, int T)
+  {
+    const size_t ntot = (size_t)job->niter_total;
+    for (int i = tid; i < R * nprm * cnt; i += T) {
+      const int rk = i / cnt, c = i - rk * cnt;
+      const int r = rk / nprm, k = rk - r * nprm;
+      if (!lay.active(r)) continue;
+      job->pout[(((size_t)k * nbeta + lay.ibeta(r)) * nseq + lay.iseq(r)) * ntot + col0 + c] =
+          st_p[rk * kCH + c];
+    }
+  }
+  __device__ void stage_exchange(int slot, int tid, int T)
+  {
+    for (int s = tid; s < nbeta; s += T) st_t[s * kCH + slot] = x_tcur[s];
+    if (tid == 0) st_c[slot] = x_chi2[0];
+  }
+  __device__ void flush_exchange(int iseq, int cnt, size_t col0, int tid, int T)
+  {
+    const size_t ntot = (size_t)job->niter_total;
+    for (int i = tid; i < nbeta * cnt; i += T) {
+      const int s = i / cnt, c = i - s * cnt;
+      job->tout[((size_t)s * nseq + iseq) * ntot + col0 + c] = st_t[s * kCH + c];
+    }
+    for (int c = tid; c < cnt; c += T) job->chi2[(size_t)iseq * ntot + col0 + c] = st_c[c];
+  }
+
+  // ---- write-back ------------------------------------------------------------------
+  template <class Lay>
+  __device__ void store_rows(const Lay &lay, int tid, int T)
+  {
+    for (int i = tid; i < R * nptot; i += T) {
+      const int r = i / nptot, j = i - r * nptot;
+      if (!lay.active(r)) continue;
+      const int ist = lay.ibeta(r) * nseq + lay.iseq(r);
+      job->pcur[(size_t)ist * nptot + j] = params[i];
+    }
+    for (int i = tid; i < R * nprm; i += T) {
+      const int r = i / nprm, k = i - r * nprm;
+      if (!lay.active(r)) continue;
+      const int ibeta = lay.ibeta(r), iseq = lay.iseq(r);
+      const size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
+      job->pstp[gi] = s_pstp[i];
+      job->n_cnt[gi] = s_ncnt[i];
+      job->n_acpt[gi] = s_nacpt[i];
+      if (!s_hslow[i] && job->nburn > 0) {
+        for (int a = 0; a < nadj; ++a)
+          job->n_hist[(((size_t)nprm * a + k) * nbeta + ibeta) * nseq + iseq] =
+              (s_hbits[i * HW + (a >> 5)] >> (a & 31)) & 1u;
+      }
+    }
+  }
+  __device__ void store_exchange(int iseq, int tid, int T)
+  {
+    for (int s = tid; s < nbeta; s += T) {
+      job->tcur[s * nseq + iseq] = x_tcur[s];
+      job->n_exch[s * nseq + iseq] = x_nexch[s];
+    }
+  }
+  template <class Lay>
+  __device__ void store_slot(const Lay &lay, int r, const Rng &rng)
+  {
+    if (!lay.active(r)) return;
+    const int ist = lay.ibeta(r) * nseq + lay.iseq(r);
+    job->chi2c[ist] = s_chi2c[r];
+    job->flag[ist] = s_flag[r];
+    job->ptent[ist] = s_ptent[r];
+    job->ptentn[ist] = s_ptentn[r];
+    if (rng.inj) {
+      job->inj_cur[2 * ist] = rng.cu;
+      job->inj_cur[2 * ist + 1] = rng.cn;
+    } else {
+      reinterpret_cast<curandStateXORWOW *>(job->rndst)[ist] = rng.st;
+    }
+    if (rng.ovf) set_status(job->status, CMC_ERR_STREAM);
+  }
+};
+
+// ---- the spread layout's exchange through global memory ------------------------------
+// Run by all T threads of the CTA after the slot threads accepted their last
+// proposals.  1. every CTA publishes its rows and chi^2 (double buffered by
+// iteration parity), fences, and counts in at each sequence it holds
+// (release); 2. the owner waits (acquire) for (iteration + 1) x the CTAs
+// holding its sequence, runs the nbeta attempts, writes the permutation and
+// the permuted chi^2 and stores done = iteration + 1 (release); 3. every CTA
+// waits for done of its sequences and pulls its new rows.  Deadlock-free by
+// induction over iterations (arrivals never wait; an owner's wait needs only
+// this iteration's arrivals, which need only the previous iteration's done;
+// all CTAs are resident).  A buffer is rewritten two iterations later, after
+// each of its readers has arrived at the iteration in between.  Returns false
+// after an abort (a wait ran out).
+template <class Model, int R>
+__device__ bool spread_exchange(SweepState<Model, R> &S, const SpreadLayout &lay,
+                                const SpreadCtl &ctl, int iter, bool burn, Rng &rng, int tid,
+                                int T, int *s_ok)
+{
+  using AtomicInt = cuda::atomic_ref<int, cuda::thread_scope_device>;
+  const int nbeta = S.nbeta, nptot = S.nptot;
+  const size_t nrep = (size_t)nbeta * S.nseq, par = (size_t)(iter & 1);
+  float *xp = ctl.xp + par * nrep * nptot;
+  float *xc = ctl.xc + par * nrep;
+  int *xperm = ctl.xperm + par * nrep;
+  float *xchi = ctl.xchi + par * nrep;
+  const int cnt = lay.cnt;
+  __syncthreads();   // the last accept_adjust may have restored a row
+  for (int i = tid; i < cnt * nptot; i += T) xp[(size_t)lay.gstart * nptot + i] = S.params[i];
+  for (int r = tid; r < cnt; r += T) xc[lay.gstart + r] = S.s_chi2c[r];
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    for (int s = lay.seq_lo; s <= lay.seq_hi; ++s)
+      AtomicInt(ctl.arrive[s]).fetch_add(1, cuda::memory_order_release);
+  }
+  if (lay.owner() && tid < 32) {
+    const int s = lay.own_seq();
+    int ok = 1;
+    if (tid == 0) {
+      ok = spin_until_geq(&ctl.arrive[s], (iter + 1) * lay.own_ncta, ctl.abort, S.job->status);
+      __threadfence();
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (ok) {
+      const float chi = (tid < nbeta) ? __ldcg(&xc[(size_t)s * nbeta + tid]) : 0.0f;
+      warp_exchange(chi, burn, rng, lay.own_slot(), nbeta, S.x_beta, S.x_chi2, S.x_tcur,
+                    S.x_perm, S.x_nexch, S.job->status);
+      if (tid < nbeta) {
+        xperm[(size_t)s * nbeta + tid] = S.x_perm[tid];
+        xchi[(size_t)s * nbeta + tid] = S.x_chi2[tid];
+      }
+      __threadfence();
+      __syncwarp();
+      if (tid == 0 && s != ctl.hold)
+        AtomicInt(ctl.done[s]).store(iter + 1, cuda::memory_order_release);
+    }
+  }
+  if (tid == 0) {
+    int ok = 1;
+    for (int s = lay.seq_lo; s <= lay.seq_hi && ok; ++s)
+      ok = spin_until_geq(&ctl.done[s], iter + 1, ctl.abort, S.job->status) ? 1 : 0;
+    __threadfence();
+    *s_ok = ok;
+  }
+  __syncthreads();
+  if (!*s_ok) return false;
+  for (int i = tid; i < cnt * nptot; i += T) {
+    const int r = i / nptot, j = i - r * nptot, f = lay.gstart + r;
+    const int src = __ldcg(&xperm[f]);
+    S.params[i] = __ldcg(&xp[((size_t)(f - f % nbeta) + src) * nptot + j]);
+  }
+  for (int r = tid; r < cnt; r += T) S.s_chi2c[r] = __ldcg(&xchi[lay.gstart + r]);
+  __syncthreads();
+  return true;
+}
+
+// ---- cluster and spread layouts: one body for all R slots ---------------------------
+
+// The replicas of layout `lay` on the calling CTA (in the cluster layout, all
+// CTAs of the cluster call this with the same sequence).  `smem` is the CTA's
+// dynamic shared memory, at least make_plan(...).total bytes for this job;
+// `ctl` is used by the spread layout only.
+template <class Model, int R, class Lay>
+__device__ void run_replicas(const cmc_job &job, const typename Model::Packed &pk, const Lay &lay,
+                             const SpreadCtl &ctl, unsigned char *smem)
+{
+  const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
+  const int nbeta = job.nbeta, nseq = job.nseq, nptot = job.nptot, nprm = job.nprm;
+
+  const SmemPlan P = make_plan(R, T, nptot, nprm, nbeta, job.nadj, sizeof(typename Model::Consts),
+                               Model::scratch_bytes(pk, R));
+  SweepState<Model, R> S;
+  S.bind(job, P, smem, NW);
+  __shared__ int s_ok;
+
+  Cta<Model, R> cta;
+  cta.job = &job;
+  cta.pk = &pk;
+  cta.consts = S.s_consts;
+  cta.flag = S.s_flag;
+  cta.scratch = S.scratch;
+  cta.tid = tid;
+  cta.nthreads = T;
+#pragma unroll
+  for (int r = 0; r < R; ++r) cta.ist[r] = lay.active(r) ? lay.ibeta(r) * nseq + lay.iseq(r) : 0;
+  cta.ph_region = lay.ph_region(nbeta);
+
+  // ---- load tables and state ------------------------------------------------
+  S.load_tables(tid, T);
+  S.load_rows(lay, tid, T);
+  if (lay.owner()) S.load_exchange(lay.own_seq(), tid, T);
+  Rng rng;
+  if (tid < R) S.load_slot(lay, tid, rng);
+  Model::setup(cta, tid, T);
+  __syncthreads();
+
+  // ---- init_pcur + first chi^2 (src/gpu_mcmc.cu:245-267, 714-719) ---------
+  if (job.do_init) {
+    if (tid < R && lay.active(tid)) S.init_slot(tid, rng, cta);
+    __syncthreads();
+    float acc[R];
+    Model::template eval<R>(cta, acc);
+    block_reduce<Model, R>(acc, S.s_red, tid, NW);
+    __syncthreads();
+    if (tid < R && lay.active(tid)) S.s_chi2c[tid] = S.red_sum(tid);
+    __syncthreads();
+  }
+
+  // The accept step of proposal n is fused with proposal n+1 on the slot's
+  // thread, so that one barrier per proposal disappears.
   const int nsteps = job.nburn + job.niter;
   for (int step = 0; step < nsteps; ++step) {
     const bool burn = step < job.nburn;
     for (int ipm = 0; ipm < nprm; ++ipm) {
-      if (tid < nact) {
+      if (tid < R && lay.active(tid)) {
         const int r = tid;
-        if (ipm > 0) accept_adjust(r, burn);
-        if (block) {
-          block_proposal(r);
-        } else {
-          // gen_proposal (src/gpu_mcmc.cu:361-411)
-          const int k = rng.index(nprm, job.status);
-          const int t = s_ivar[k];
-          float p = params[r * nptot + t];
-          s_k[r] = k;
-          s_ptentn[r] = t;
-          s_ptent[r] = p;
-          const float sd = s_pstp[r * nprm + k];
-          const float rn = rng.normal();
-          p = __fmaf_rn(sd, rn, p);
-          if (s_pdescr[t] == 2) p = wrap_pi(p);
-          if ((p < s_pmin[t]) || (p > s_pmax[t])) {
-            s_flag[r] = 0;
-          } else {
-            s_flag[r] = 1;
-            params[r * nptot + t] = p;
-            for (int j = 0; j < nptot; ++j) plast[r * nptot + j] = params[r * nptot + j];
-            Model::prepare(cta, r, &params[r * nptot]);
-            s_evald[r] = 1;
-          }
-        }
+        if (ipm > 0) S.accept_adjust(r, burn, lay.ibeta(r), lay.iseq(r), rng);
+        S.propose(r, lay.iseq(r), rng, cta);
       }
       __syncthreads();
       // calc_chi2_terms x npass + the chi^2 sum (src/gpu_mcmc.cu:273-325, 447-448)
       float acc[R];
       Model::template eval<R>(cta, acc);
-      block_reduce<Model, R>(acc, s_red, tid, NW);
+      block_reduce<Model, R>(acc, S.s_red, tid, NW);
       __syncthreads();
     }
-    if (tid < nact) accept_adjust(tid, burn);
+    if (tid < R && lay.active(tid)) S.accept_adjust(tid, burn, lay.ibeta(tid), lay.iseq(tid), rng);
 
     // ---- replica_exchange (src/gpu_mcmc.cu:533-626) ------------------------
     // nbeta attempts in the reference's order, drawn from the ibeta = 0
@@ -450,11 +694,13 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
     if constexpr (!Lay::kSpread) {
       cg::cluster_group cluster = cg::this_cluster();
       const int rank = lay.rank;
+      float *x_chi2 = S.x_chi2, *x_beta = S.x_beta;
+      int *x_perm = S.x_perm, *x_tcur = S.x_tcur, *x_nexch = S.x_nexch;
       cluster.sync();
       if (nbeta <= 32) {
         if (rank == 0 && tid < 32) {
           const float chi =
-              (tid < nbeta) ? cluster.map_shared_rank(s_chi2c, tid / R)[tid % R] : 0.0f;
+              (tid < nbeta) ? cluster.map_shared_rank(S.s_chi2c, tid / R)[tid % R] : 0.0f;
           warp_exchange(chi, burn, rng, 0, nbeta, x_beta, x_chi2, x_tcur, x_perm, x_nexch,
                         job.status);
         }
@@ -462,7 +708,7 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
         if (rank == 0) {
           // gather the nbeta chi^2 values in parallel (one remote load each)
           for (int s = tid; s < nbeta; s += T) {
-            x_chi2[s] = cluster.map_shared_rank(s_chi2c, s / R)[s % R];
+            x_chi2[s] = cluster.map_shared_rank(S.s_chi2c, s / R)[s % R];
             x_perm[s] = s;
           }
           __syncthreads();
@@ -491,74 +737,19 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
         for (int i = tid; i < R * nptot; i += T) {
           int r = i / nptot, j = i - r * nptot;
           int src = perm0[rank * R + r];
-          const float *rp = cluster.map_shared_rank(params, src / R);
-          ptmp[i] = rp[(src % R) * nptot + j];
+          const float *rp = cluster.map_shared_rank(S.params, src / R);
+          S.ptmp[i] = rp[(src % R) * nptot + j];
         }
-        if (tid < R) ptmp[R * nptot + tid] = chi0[rank * R + tid];
+        if (tid < R) S.ptmp[R * nptot + tid] = chi0[rank * R + tid];
       }
       cluster.sync();
-      for (int i = tid; i < R * nptot; i += T) params[i] = ptmp[i];
-      if (tid < R) s_chi2c[tid] = ptmp[R * nptot + tid];
+      for (int i = tid; i < R * nptot; i += T) S.params[i] = S.ptmp[i];
+      if (tid < R) S.s_chi2c[tid] = S.ptmp[R * nptot + tid];
       __syncthreads();
     } else {
-      // Publish this CTA's replicas, count in at their sequences, let each
-      // sequence's owner run the exchange, and pull the new rows.  The waits
-      // are bounded (spin_until_geq); after an abort every CTA leaves the
-      // iteration loop and writes its state back with the error status set.
-      using AtomicInt = cuda::atomic_ref<int, cuda::thread_scope_device>;
-      const size_t nrep = (size_t)nbeta * nseq, par = (size_t)(step & 1);
-      float *xp = ctl.xp + par * nrep * nptot;
-      float *xc = ctl.xc + par * nrep;
-      int *xperm = ctl.xperm + par * nrep;
-      float *xchi = ctl.xchi + par * nrep;
-      __syncthreads();   // the last accept_adjust may have restored a row
-      for (int i = tid; i < nact * nptot; i += T) xp[(size_t)lay.start * nptot + i] = params[i];
-      if (tid < nact) xc[lay.start + tid] = s_chi2c[tid];
-      __threadfence();
-      __syncthreads();
-      if (tid == 0) {
-        __threadfence();
-        for (int s = lay.seq_lo; s <= lay.seq_hi; ++s)
-          AtomicInt(ctl.arrive[s]).fetch_add(1, cuda::memory_order_release);
-      }
-      if (lay.owner() && tid < 32) {
-        const int s = lay.own_seq();
-        int ok = 1;
-        if (tid == 0) {
-          ok = spin_until_geq(&ctl.arrive[s], (step + 1) * lay.own_ncta, ctl.abort, job.status);
-          __threadfence();
-        }
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (ok) {
-          const float chi = (tid < nbeta) ? __ldcg(&xc[(size_t)s * nbeta + tid]) : 0.0f;
-          warp_exchange(chi, burn, rng, lay.own_slot(), nbeta, x_beta, x_chi2, x_tcur, x_perm,
-                        x_nexch, job.status);
-          if (tid < nbeta) {
-            xperm[(size_t)s * nbeta + tid] = x_perm[tid];
-            xchi[(size_t)s * nbeta + tid] = x_chi2[tid];
-          }
-          __threadfence();
-          __syncwarp();
-          if (tid == 0 && s != ctl.hold)
-            AtomicInt(ctl.done[s]).store(step + 1, cuda::memory_order_release);
-        }
-      }
-      if (tid == 0) {
-        int ok = 1;
-        for (int s = lay.seq_lo; s <= lay.seq_hi && ok; ++s)
-          ok = spin_until_geq(&ctl.done[s], step + 1, ctl.abort, job.status) ? 1 : 0;
-        __threadfence();
-        s_ok = ok;
-      }
-      __syncthreads();
-      if (!s_ok) break;
-      for (int i = tid; i < nact * nptot; i += T) {
-        const int r = i / nptot, j = i - r * nptot, f = lay.start + r;
-        const int src = __ldcg(&xperm[f]);
-        params[i] = __ldcg(&xp[((size_t)(f - f % nbeta) + src) * nptot + j]);
-      }
-      if (tid < nact) s_chi2c[tid] = __ldcg(&xchi[lay.start + tid]);
-      __syncthreads();
+      // after an abort every CTA leaves the iteration loop and writes its
+      // state back with the error status set
+      if (!spread_exchange<Model, R>(S, lay, ctl, step, burn, rng, tid, T, &s_ok)) break;
     }
     Model::after_exchange(cta);
 
@@ -566,83 +757,30 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
     if (!burn) {
       const int m = step - job.nburn;
       const int slot = m % kCH;
-      for (int i = tid; i < R * nprm; i += T) {
-        int r = i / nprm, k = i - r * nprm;
-        st_p[i * kCH + slot] = params[r * nptot + s_ivar[k]];
-      }
-      if (lay.owner()) {
-        for (int s = tid; s < nbeta; s += T) st_t[s * kCH + slot] = x_tcur[s];
-        if (tid == 0) st_c[slot] = x_chi2[0];
-      }
+      S.stage_rows(slot, tid, T);
+      if (lay.owner()) S.stage_exchange(slot, tid, T);
       if (slot == kCH - 1 || m == job.niter - 1) {
         __syncthreads();
-        const int cnt = slot + 1;
         const size_t col0 = (size_t)job.itr0 + (m - slot);
-        const size_t ntot = (size_t)job.niter_total;
-        for (int i = tid; i < nact * nprm * cnt; i += T) {
-          int rk = i / cnt, c = i - rk * cnt;
-          int r = rk / nprm, k = rk - r * nprm;
-          job.pout[(((size_t)k * nbeta + lay.ibeta(r)) * nseq + lay.iseq(r)) * ntot + col0 + c] =
-              st_p[rk * kCH + c];
-        }
-        if (lay.owner()) {
-          const int iseq = lay.own_seq();
-          for (int i = tid; i < nbeta * cnt; i += T) {
-            int s = i / cnt, c = i - s * cnt;
-            job.tout[((size_t)s * nseq + iseq) * ntot + col0 + c] = st_t[s * kCH + c];
-          }
-          for (int c = tid; c < cnt; c += T) job.chi2[(size_t)iseq * ntot + col0 + c] = st_c[c];
-        }
+        S.flush_rows(lay, slot + 1, col0, tid, T);
+        if (lay.owner()) S.flush_exchange(lay.own_seq(), slot + 1, col0, tid, T);
       }
       __syncthreads();
     }
   }
 
   // ---- write the state back ------------------------------------------------
-  for (int i = tid; i < nact * nptot; i += T) {
-    int r = i / nptot, j = i - r * nptot;
-    int ist = lay.ibeta(r) * nseq + lay.iseq(r);
-    job.pcur[(size_t)ist * nptot + j] = params[i];
-  }
-  for (int i = tid; i < nact * nprm; i += T) {
-    int r = i / nprm, k = i - r * nprm, ibeta = lay.ibeta(r), iseq = lay.iseq(r);
-    size_t gi = ((size_t)k * nbeta + ibeta) * nseq + iseq;
-    job.pstp[gi] = s_pstp[i];
-    job.n_cnt[gi] = s_ncnt[i];
-    job.n_acpt[gi] = s_nacpt[i];
-    if (!s_hslow[i] && job.nburn > 0) {
-      for (int a = 0; a < nadj; ++a)
-        job.n_hist[(((size_t)nprm * a + k) * nbeta + ibeta) * nseq + iseq] =
-            (s_hbits[i * HW + (a >> 5)] >> (a & 31)) & 1u;
-    }
-  }
-  if (lay.owner()) {
-    const int iseq = lay.own_seq();
-    for (int s = tid; s < nbeta; s += T) {
-      job.tcur[s * nseq + iseq] = x_tcur[s];
-      job.n_exch[s * nseq + iseq] = x_nexch[s];
-    }
-  }
-  if (tid < nact) {
-    const int r = tid, ist = lay.ibeta(r) * nseq + lay.iseq(r);
-    job.chi2c[ist] = s_chi2c[r];
-    job.flag[ist] = s_flag[r];
-    job.ptent[ist] = s_ptent[r];
-    job.ptentn[ist] = s_ptentn[r];
-    if (rng.inj) {
-      job.inj_cur[2 * ist] = rng.cu;
-      job.inj_cur[2 * ist + 1] = rng.cn;
-    } else {
-      reinterpret_cast<curandStateXORWOW *>(job.rndst)[ist] = rng.st;
-    }
-    if (rng.ovf) set_status(job.status, CMC_ERR_STREAM);
-  }
+  S.store_rows(lay, tid, T);
+  if (lay.owner()) S.store_exchange(lay.own_seq(), tid, T);
+  if (tid < R) S.store_slot(lay, tid, rng);
   // Model rows of each replica's last evaluation (datm / chi2m outputs).
-  Model::template final_rows<R>(cta, plast, s_evald);
+  Model::template final_rows<R>(cta, S.plast, S.s_evald);
   // No CTA may leave (or start its next sequence) while another can still
   // read its shared memory.
   if constexpr (!Lay::kSpread) cg::this_cluster().sync();
 }
+
+// ---- kernels ------------------------------------------------------------------------
 
 // One launch for one job: cluster c runs sequence c.  (The kernel bodies are
 // device functions so that a model compiled into a loadable module can wrap
@@ -675,24 +813,8 @@ __device__ __forceinline__ void spread_body(const cmc_job &job, const typename M
                                             const SpreadCtl &ctl)
 {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int nbeta = job.nbeta, nrep = nbeta * job.nseq, N = (int)gridDim.x;
-  SpreadLayout lay;
-  lay.nbeta = nbeta;
-  spread_range(nrep, N, (int)blockIdx.x, lay.start, lay.cnt);
-  lay.seq_lo = lay.start / nbeta;
-  lay.seq_hi = (lay.start + lay.cnt - 1) / nbeta;
-  lay.own = -1;
-  lay.own_r = 0;
-  if (lay.start % nbeta == 0) {
-    lay.own = lay.seq_lo;
-  } else if (lay.seq_hi > lay.seq_lo) {
-    lay.own = lay.seq_hi;
-    lay.own_r = lay.seq_hi * nbeta - lay.start;
-  }
-  lay.region0 = (int)blockIdx.x * R;
-  lay.own_ncta = 0;
-  if (lay.own >= 0)
-    lay.own_ncta = spread_cta_of(nrep, N, lay.own * nbeta + nbeta - 1) - (int)blockIdx.x + 1;
+  const SpreadLayout lay = make_spread_layout(job.nbeta, job.nseq, (int)gridDim.x,
+                                              (int)blockIdx.x, (int)blockIdx.x * R);
   run_replicas<Model, R>(job, pk, lay, ctl, smem);
 }
 

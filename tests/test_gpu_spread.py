@@ -182,3 +182,4 @@ def test_spread_wait_that_runs_out_reports_timeout(monkeypatch):
     _, a = _run(w, dict(R=8, T=128, phasor=0, layout=1), nburn=2, niter=2)
     _, b = _run(w, shape, nburn=2, niter=2)
     _same(a, b)
+
