@@ -19,7 +19,7 @@
 // array compiled into this library (kStaticWorkBytes = 4 MiB).  The packed
 // data takes 52 bytes per point and 32 per closure, so at most about 80,000
 // points; the closure phases of all replicas then need the rest of the array
-// (nbeta*nseq*points*4 bytes, used from 2048 points on) or, failing that,
+// ((nbeta*nseq + 8)*points*4 bytes, used from 2048 points on) or, failing that,
 // shared memory (R*points*4 bytes per CTA, R >= nbeta/16: up to about 27,000
 // points at 32 temperatures).  Where cmc_run with a full job->work would keep
 // the phases in global memory and they do not fit in the array, this call
@@ -75,7 +75,7 @@ extern "C" int cmc_run_noalloc(const cmc_job *job, void *stream)
   j.work = p;
   j.work_bytes = kStaticWorkBytes;
   // The closure phases of every replica must fit too: beside the packed data
-  // in the array (from 2048 points on, when nbeta*nseq*points floats fit
+  // in the array (from 2048 points on, when (nbeta*nseq + 8)*points floats fit
   // there) or else in shared memory, where each CTA keeps the phases of its
   // R >= nbeta/16 replicas.  A job that fits neither is refused here with a
   // message that names the array.
@@ -90,7 +90,7 @@ extern "C" int cmc_run_noalloc(const cmc_job *job, void *stream)
     if (cmc::pick_sweep_config<cmc::SgraModel>(j, pk, c) != CMC_OK)
       return cmc::fail(CMC_ERR_UNSUPPORTED,
                        "cmc_run_noalloc: the closure phases of this job fit neither beside "
-                       "the packed data in the fixed 4 MiB array (nbeta*nseq*points*4 bytes) "
+                       "the packed data in the fixed 4 MiB array ((nbeta*nseq + 8)*points*4 bytes) "
                        "nor in shared memory (R*points*4 bytes per CTA with R >= nbeta/16 "
                        "replicas); use cmc_run with job->work of cmc_work_bytes() bytes");
   }

@@ -104,7 +104,7 @@ int cmc_run(const cmc_job *job, void *stream);
  * from a fixed 4 MiB array inside the library instead.  Limits: the packed
  * data (52 bytes per point + 32 per closure: at most about 80,000 points,
  * else CMC_ERR_ARG), and the closure phases of all replicas either beside it
- * in the array (nbeta*nseq*points*4 bytes, from 2048 points on) or else in
+ * in the array ((nbeta*nseq + 8)*points*4 bytes, from 2048 points on) or else in
  * shared memory (R*points*4 bytes per CTA with R >= nbeta/16: up to about
  * 27,000 points at 32 temperatures), else CMC_ERR_UNSUPPORTED.  A large job
  * whose phases cmc_run would keep in a full job->work may therefore run here
