@@ -11,11 +11,15 @@
 //   * every thread of the CTA evaluates the model for all R replicas over a
 //     strided share of the data; per-replica chi^2 partials are reduced with
 //     warp shuffles and a fixed-order shared-memory pass (deterministic);
-//   * the replica exchange of a sequence runs on cluster rank 0, thread 0,
+//   * the replica exchange of a sequence runs on warp 0 of cluster rank 0,
 //     with the ibeta = 0 replica's generator, over chi^2 values gathered from
 //     the other CTAs through distributed shared memory; the winning
 //     permutation is then applied by every CTA pulling its new parameter
 //     rows from their owners (DSMEM), between cluster barriers.
+// The spread layout (cmc_sweep.cuh) instead shares all replicas evenly among
+// the CTAs of one cooperative launch, R or R-1 each, and runs each
+// sequence's exchange on the CTA holding its ibeta = 0 replica through
+// global memory.
 //
 // The algorithm is the reference's (src/gpu_mcmc.cu):
 //   init_rng :228-239, init_pcur :245-267, gen_proposal :361-411,
