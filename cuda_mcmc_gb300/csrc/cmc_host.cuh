@@ -217,10 +217,11 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         if (n <= 0) continue;
         const int waves = (j.nseq + n - 1) / n;
         // Measured on GB300, lexicographic, lower is better.  With phases in
-        // global memory, first whether the resident replicas' phase regions
-        // fit in three quarters of L2 (20000 visibilities: 36 resident
-        // clusters of 32 replicas, 92 MB, in two waves beat 64 clusters,
-        // 164 MB, in one by 7 %: the larger set spills to DRAM).  Then fewest
+        // global memory, first whether the resident replicas' phases fit in
+        // three quarters of L2 -- phases are kept for closure corners only,
+        // at most 3 per closure (20000 visibilities + 6000 closures: 36 or 40
+        // resident clusters of 32 replicas in two waves beat 64 clusters in
+        // one by 7 %: the larger set spills to DRAM).  Then fewest
         // waves of resident clusters.  Then, with a few data terms per replica
         // (the plugin models: ndat 1-8), the per-proposal serial work of a
         // CTA's R replicas is the time: fewest replicas per CTA, then fewest
@@ -229,12 +230,17 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         // replica (16 or 64 cost ~10 %); then the phase storage (phasors,
         // phases in shared memory, phases in global memory: an L2 round trip
         // per closure gather); then more replicas per CTA (more independent
-        // work per thread), except with phases in global memory, where 4
-        // replicas per CTA do best (20000 visibilities: R=4 T=128 11.1 ms,
-        // R=8 T=256 12.7 ms per 4 iterations).
+        // work per thread), except with phases in global memory, where the
+        // point data stream from L2 (loaded two points ahead up to R = 4)
+        // and 2, then 4, replicas per CTA do best (20000 + 6000, 10
+        // iterations: R=2 T=128 21.7 ms, R=4 T=256 22.8 ms, R=4 T=128 23.0
+        // ms; R=8 T=256 12.7 ms against R=4 T=128 11.1 ms per 4 iterations).
         double phase_set = 0.0;
         if constexpr (Model::kGlobalPhases) {
-          if (ph == 2) phase_set = (double)std::min(n, j.nseq) * j.nbeta * (double)q.npts * 4.0;
+          if (ph == 2) {
+            const int corners = (q.ncph > 0 && q.npass >= 2) ? std::min(q.npts, 3 * q.ncph) : 0;
+            phase_set = (double)std::min(n, j.nseq) * j.nbeta * (double)corners * 4.0;
+          }
         }
         const int spill = (ph == 2 && l2_budget > 0.0 && phase_set > l2_budget) ? 1 : 0;
         double score = spill * 100000.0;
@@ -251,7 +257,8 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
               small ? ((tpr == 64) ? 0 : (tpr == 32 || tpr == 128) ? 1 : 2)
                     : ((tpr == 32) ? 0 : (tpr == 64 || tpr == 16) ? 1 : 2);
           const int store_rank = (ph == 1) ? 0 : (ph == 0) ? 1 : 2;
-          const double r_rank = (ph == 2) ? (double)std::abs(R - 4) : -(double)R;
+          const double r_rank =
+              (ph == 2) ? ((R == 2) ? 0.0 : (R == 4) ? 1.0 : 2.0 + std::abs(R - 4)) : -(double)R;
           score += waves * 1000.0 + shape_rank * 100.0 + store_rank * 10.0 + r_rank;
         }
         if (score < best - 1e-9) {

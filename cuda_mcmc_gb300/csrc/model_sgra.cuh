@@ -470,21 +470,35 @@ struct SgraModel {
       }
     };
     // The next point's data is loaded one iteration ahead (its L2 latency
-    // overlaps this point's terms when the data set outgrows L1).
+    // overlaps this point's terms when the data set outgrows L1), two ahead
+    // with phases in global memory and up to 4 replicas per CTA (large data
+    // sets, whose points stream from L2 behind the phase traffic, at the
+    // replica counts where the registers allow it).
+    constexpr int kAhead = (GL && R <= 4) ? 2 : 1;
     const int nused = cta.model_i;
     int i = tid;
-    float4 dn = make_float4(0.f, 0.f, 0.f, 0.f);
-    float rn = 0.0f;
-    if (i < npts) {
-      dn = __ldg(&pk.vis[i]);
-      rn = __ldg(&pk.rho[i]);
+    float4 dn[kAhead];
+    float rn[kAhead];
+#pragma unroll
+    for (int a = 0; a < kAhead; ++a) {
+      dn[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+      rn[a] = 0.0f;
+      if (i + a * T < npts) {
+        dn[a] = __ldg(&pk.vis[i + a * T]);
+        rn[a] = __ldg(&pk.rho[i + a * T]);
+      }
     }
     auto next = [&](int i, float4 &d, float &rho) {
-      d = dn;
-      rho = rn;
-      if (i + T < npts) {
-        dn = __ldg(&pk.vis[i + T]);
-        rn = __ldg(&pk.rho[i + T]);
+      d = dn[0];
+      rho = rn[0];
+#pragma unroll
+      for (int a = 0; a + 1 < kAhead; ++a) {
+        dn[a] = dn[a + 1];
+        rn[a] = rn[a + 1];
+      }
+      if (i + kAhead * T < npts) {
+        dn[kAhead - 1] = __ldg(&pk.vis[i + kAhead * T]);
+        rn[kAhead - 1] = __ldg(&pk.rho[i + kAhead * T]);
       }
     };
     for (; i < nused; i += T) {
