@@ -15,7 +15,7 @@ _libs = {}
 _lock = threading.Lock()
 
 CMC_OK, CMC_ERR_ARG, CMC_ERR_CUDA, CMC_ERR_STREAM, CMC_ERR_MODEL, CMC_ERR_NOMEM, \
-    CMC_ERR_UNSUPPORTED, CMC_ERR_TIMEOUT = range(8)
+    CMC_ERR_UNSUPPORTED, CMC_ERR_TIMEOUT, CMC_ERR_CANCELLED = range(9)
 CMC_RNG_CURAND, CMC_RNG_INJECTED = 0, 1
 CMC_PROP_SINGLE, CMC_PROP_BLOCK = 0, 1
 MODE_MODCHI2, MODE_MODEL = 1, 2
@@ -74,6 +74,7 @@ EXPORTS = ("mcmc_cuda", "mcmc_cuda_v2", "calc_modchi2", "calc_modchi2_v2", "calc
            "cmc_query_config", "cmc_set_config", "cmc_set_layout", "cmc_batch_work_bytes",
            "cmc_batch_prepare",
            "cmc_batch_run", "cmc_batch_info", "cmc_batch_free", "cmc_batch_run_class",
+           "cmc_batch_cancel",
            "cmc_batch_set_class")
 
 
@@ -120,6 +121,8 @@ def _declare(L):
     L.cmc_batch_info.restype = C.c_int
     L.cmc_batch_free.argtypes = [C.c_void_p]
     L.cmc_batch_free.restype = None
+    L.cmc_batch_cancel.argtypes = [C.c_void_p]
+    L.cmc_batch_cancel.restype = C.c_int
     L.cmc_batch_run_class.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_void_p]
     L.cmc_batch_run_class.restype = C.c_int

@@ -511,10 +511,16 @@ struct BatchPlan {
   cmc_job *jobs_dev = nullptr;
   void *pks_dev = nullptr;
   int2 *items_dev = nullptr;
-  int *counters_dev = nullptr;
+  int *counters_dev = nullptr;      // [class][2]: work-list counter, cancel flag
+  int *cancel_src = nullptr;        // pinned host values the cancel copies from (a copy
+                                    // from pinned memory runs beside running launches)
   std::vector<cmc_job> jobs;        // host copies (kept for the uploads)
   std::vector<unsigned char> pks;   // host copies of the packed descriptors
   std::vector<int2> items;
+  ~BatchPlan()
+  {
+    if (cancel_src) cudaFreeHost(cancel_src);
+  }
 };
 
 constexpr int kBatchMaxClasses = 4;
@@ -527,7 +533,7 @@ size_t batch_work_bytes(const cmc_job *jobs, int n)
   for (int i = 0; i < n; ++i) items += (size_t)std::max(jobs[i].nseq, 0);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   return al(sizeof(cmc_job) * n) + al(sizeof(typename Model::Packed) * n) + al(8 * items) +
-         al(4 * kBatchMaxClasses);
+         al(8 * kBatchMaxClasses);
 }
 
 template <class Model>
@@ -669,7 +675,14 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
   P->pks_dev = (void *)(w + o);       o += al(sizeof(Packed) * n);
   P->items_dev = (int2 *)(w + o);     o += al(8 * P->items.size());
   P->counters_dev = (int *)(w + o);
-  cudaError_t e = cudaMemcpyAsync(P->jobs_dev, P->jobs.data(), sizeof(cmc_job) * n,
+  cudaError_t e = cudaHostAlloc(&P->cancel_src, 2 * sizeof(int), cudaHostAllocDefault);
+  if (e == cudaSuccess) {
+    P->cancel_src[0] = 1;                    // a set cancel flag
+    P->cancel_src[1] = CMC_ERR_CANCELLED;    // the jobs' status
+    e = cudaMemsetAsync(P->counters_dev, 0, 8 * kBatchMaxClasses, s);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->jobs_dev, P->jobs.data(), sizeof(cmc_job) * n,
                                   cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(P->pks_dev, P->pks.data(), sizeof(Packed) * n, cudaMemcpyHostToDevice, s);
@@ -685,8 +698,9 @@ int batch_prepare(const cmc_job *jobs, int n, void *work, size_t bytes, cudaStre
   return CMC_OK;
 }
 
-// Launches only (device-side state and work lists are ready): one memset and
-// one persistent kernel per size class, all on `s`.
+// Launches only (device-side state and work lists are ready): one memset of
+// the counters and cancel flags, then one persistent kernel per size class,
+// all on `s`.
 template <class Model>
 int batch_run(BatchPlan *P, int do_init, int nburn, int niter, int itr0, cudaStream_t s)
 {
@@ -694,13 +708,15 @@ int batch_run(BatchPlan *P, int do_init, int nburn, int niter, int itr0, cudaStr
   if (!P) return fail(CMC_ERR_ARG, "batch: plan is NULL");
   if (nburn < 0 || niter < 0 || itr0 < 0 || itr0 + niter > P->min_niter_total)
     return fail(CMC_ERR_ARG, "batch: need nburn, niter >= 0 and itr0 + niter <= niter_total");
+  // every class's work-list counter and cancel flag, once before the first
+  // launch: a cancel that lands while one class runs stops the later ones too
+  CMC_CUDA(cudaMemsetAsync(P->counters_dev, 0, 8 * kBatchMaxClasses, s));
   for (size_t c = 0; c < P->classes.size(); ++c) {
     const BatchClass &bc = P->classes[c];
-    CMC_CUDA(cudaMemsetAsync(P->counters_dev + c, 0, sizeof(int), s));
     const int rc = dispatch_R<Model>(bc.R, [&](auto rcn) {
       return launch_batch<Model, decltype(rcn)::value>(
           P->jobs_dev, reinterpret_cast<const Packed *>(P->pks_dev), P->items_dev + bc.item0,
-          bc.nitems, P->counters_dev + c, bc.G, bc.T, bc.smem, bc.nclusters, do_init, nburn,
+          bc.nitems, P->counters_dev + 2 * c, bc.G, bc.T, bc.smem, bc.nclusters, do_init, nburn,
           niter, itr0, s);
     });
     if (rc) return rc;
@@ -719,13 +735,42 @@ int batch_run_class(BatchPlan *P, int cls, int do_init, int nburn, int niter, in
   if (nburn < 0 || niter < 0 || itr0 < 0 || itr0 + niter > P->min_niter_total)
     return fail(CMC_ERR_ARG, "batch: need nburn, niter >= 0 and itr0 + niter <= niter_total");
   const BatchClass &bc = P->classes[cls];
-  CMC_CUDA(cudaMemsetAsync(P->counters_dev + cls, 0, sizeof(int), s));
+  CMC_CUDA(cudaMemsetAsync(P->counters_dev + 2 * cls, 0, 2 * sizeof(int), s));
   return dispatch_R<Model>(bc.R, [&](auto rcn) {
     return launch_batch<Model, decltype(rcn)::value>(
         P->jobs_dev, reinterpret_cast<const Packed *>(P->pks_dev), P->items_dev + bc.item0,
-        bc.nitems, P->counters_dev + cls, bc.G, bc.T, bc.smem, bc.nclusters, do_init, nburn,
+        bc.nitems, P->counters_dev + 2 * cls, bc.G, bc.T, bc.smem, bc.nclusters, do_init, nburn,
         niter, itr0, s);
   });
+}
+
+// Cancel the plan's running batch launches: sets every class's cancel flag
+// from a stream of its own, while the launches run (a cancel that lands
+// before the run's first memset is cleared by it), and CMC_ERR_CANCELLED in
+// every job's status word.
+// A cluster then takes no further (fit, sequence) item, and one in the
+// middle of an item stops after the exchange of its current iteration with
+// its state written back (records of the iterations done included); the
+// jobs are left at different iterations.  The next cmc_batch_run clears the
+// flags (the status words stay until the caller resets them).
+template <class Model>
+int batch_cancel(BatchPlan *P)
+{
+  if (!P || !P->cancel_src) return fail(CMC_ERR_ARG, "batch: plan is NULL");
+  cudaStream_t cs = nullptr;
+  CMC_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaError_t e = cudaSuccess;
+  for (size_t c = 0; c < P->classes.size() && e == cudaSuccess; ++c)
+    e = cudaMemcpyAsync(P->counters_dev + 2 * c + 1, P->cancel_src, sizeof(int),
+                        cudaMemcpyHostToDevice, cs);
+  for (int i = 0; i < P->njobs && e == cudaSuccess; ++i)
+    if (P->jobs[i].status)
+      e = cudaMemcpyAsync(P->jobs[i].status, P->cancel_src + 1, sizeof(int),
+                          cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) return cuda_fail(e, "batch: setting the cancel flags");
+  return CMC_OK;
 }
 
 // Give class `cls` the launch shape (R, T, phase mode) if every job of the

@@ -618,13 +618,22 @@ __device__ bool spread_exchange(SweepState<Model, R> &S, const SpreadLayout &lay
 
 // ---- cluster and spread layouts: one body for all R slots ---------------------------
 
+// Relaxed device-scope read of a flag another agent (a host copy) may set.
+__device__ __forceinline__ int read_flag(const int *p)
+{
+  return cuda::atomic_ref<int, cuda::thread_scope_device>(*const_cast<int *>(p))
+      .load(cuda::memory_order_relaxed);
+}
+
 // The replicas of layout `lay` on the calling CTA (in the cluster layout, all
 // CTAs of the cluster call this with the same sequence).  `smem` is the CTA's
 // dynamic shared memory, at least make_plan(...).total bytes for this job;
-// `ctl` is used by the spread layout only.
+// `ctl` is used by the spread layout only.  `cancel` (cluster layout, may be
+// null): a flag read by cluster rank 0 at every exchange; once set, the
+// cluster stops after that exchange, its records and state written back.
 template <class Model, int R, class Lay>
 __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &pk, const Lay &lay,
-                             const SpreadCtl &ctl, unsigned char *smem)
+                             const SpreadCtl &ctl, const int *cancel, unsigned char *smem)
 {
   const int tid = threadIdx.x, T = blockDim.x, NW = T >> 5;
   const int nbeta = job.nbeta, nseq = job.nseq, nptot = job.nptot, nprm = job.nprm;
@@ -633,7 +642,7 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
                                Model::scratch_bytes(pk, R));
   SweepState<Model, R> S;
   S.bind(job, P, smem, NW);
-  __shared__ int s_ok;
+  __shared__ int s_ok, s_stop;
 
   Cta<Model, R> cta;
   cta.job = &job;
@@ -691,12 +700,16 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
     // ---- replica_exchange (src/gpu_mcmc.cu:533-626) ------------------------
     // nbeta attempts in the reference's order, drawn from the ibeta = 0
     // replica's generator.
+    int stop = 0;
     if constexpr (!Lay::kSpread) {
       cg::cluster_group cluster = cg::this_cluster();
       const int rank = lay.rank;
       float *x_chi2 = S.x_chi2, *x_beta = S.x_beta;
       int *x_perm = S.x_perm, *x_tcur = S.x_tcur, *x_nexch = S.x_nexch;
       cluster.sync();
+      // one reading of the cancel flag for the whole cluster (rank 0's,
+      // read by every CTA after the next cluster barrier)
+      if (rank == 0 && tid == 0) s_stop = (cancel != nullptr && read_flag(cancel) != 0) ? 1 : 0;
       if (nbeta <= 32) {
         if (rank == 0 && tid < 32) {
           const float chi =
@@ -731,6 +744,7 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
         }
       }
       cluster.sync();
+      stop = *cluster.map_shared_rank(&s_stop, 0);
       {
         const int *perm0 = cluster.map_shared_rank(x_perm, 0);
         const float *chi0 = cluster.map_shared_rank(x_chi2, 0);
@@ -759,7 +773,7 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
       const int slot = m % kCH;
       S.stage_rows(slot, tid, T);
       if (lay.owner()) S.stage_exchange(slot, tid, T);
-      if (slot == kCH - 1 || m == job.niter - 1) {
+      if (slot == kCH - 1 || m == job.niter - 1 || stop) {
         __syncthreads();
         const size_t col0 = (size_t)job.itr0 + (m - slot);
         S.flush_rows(lay, slot + 1, col0, tid, T);
@@ -767,6 +781,7 @@ __device__ void run_replicas(const cmc_job &job, const typename Model::Packed &p
       }
       __syncthreads();
     }
+    if (stop) break;
   }
 
   // ---- write the state back ------------------------------------------------
@@ -793,7 +808,7 @@ __device__ __forceinline__ void sweep_body(const cmc_job &job, const typename Mo
   ClusterLayout<R> lay;
   lay.rank = (int)cluster.block_rank();
   lay.seq = blockIdx.x / (int)cluster.num_blocks();
-  run_replicas<Model, R>(job, pk, lay, SpreadCtl{}, smem);
+  run_replicas<Model, R>(job, pk, lay, SpreadCtl{}, nullptr, smem);
 }
 
 template <class Model, int R>
@@ -815,7 +830,7 @@ __device__ __forceinline__ void spread_body(const cmc_job &job, const typename M
   extern __shared__ __align__(16) unsigned char smem[];
   const SpreadLayout lay = make_spread_layout(job.nbeta, job.nseq, (int)gridDim.x,
                                               (int)blockIdx.x, (int)blockIdx.x * R);
-  run_replicas<Model, R>(job, pk, lay, ctl, smem);
+  run_replicas<Model, R>(job, pk, lay, ctl, nullptr, smem);
 }
 
 template <class Model, int R>
@@ -830,6 +845,9 @@ spread_kernel(const cmc_job job, const typename Model::Packed pk, const SpreadCt
 // counter (the list is sorted by decreasing cost, so the tail is short),
 // copies that job's descriptor into shared memory, applies this launch's
 // iteration window (do_init, nburn, niter, itr0) and runs the sequence.
+// counter[0] is the work-list counter, counter[1] the cancel flag
+// (cmc_batch_cancel): once it is set no cluster takes another item and a
+// running one stops after its next exchange.
 template <class Model, int R>
 __device__ __forceinline__ void batch_body(const cmc_job *jobs, const typename Model::Packed *pks,
                                            const int2 *items, int nitems, int *counter,
@@ -842,7 +860,8 @@ __device__ __forceinline__ void batch_body(const cmc_job *jobs, const typename M
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   for (;;) {
-    if (rank == 0 && threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    if (rank == 0 && threadIdx.x == 0)
+      s_item = (read_flag(counter + 1) != 0) ? nitems : atomicAdd(counter, 1);
     cluster.sync();
     const int it = *cluster.map_shared_rank(&s_item, 0);
     cluster.sync();
@@ -867,7 +886,7 @@ __device__ __forceinline__ void batch_body(const cmc_job *jobs, const typename M
     ClusterLayout<R> lay;
     lay.rank = rank;
     lay.seq = w.y;
-    run_replicas<Model, R>(s_job, s_pk, lay, SpreadCtl{}, smem);
+    run_replicas<Model, R>(s_job, s_pk, lay, SpreadCtl{}, counter + 1, smem);
   }
 }
 

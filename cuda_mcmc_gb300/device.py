@@ -353,6 +353,15 @@ class BatchJob:
                                                 int(niter), i0, C.c_void_p(s.cuda_stream)))
         self.itr_done = i0 + int(niter)
 
+    def cancel(self):
+        """Stop the running batch launches (callable from another host thread
+        while they run): no cluster takes a further (fit, sequence) item, a
+        running one stops after its current iteration's exchange with its
+        state and records written back, and every job's status becomes
+        CMC_ERR_CANCELLED (its check() raises; the jobs are left at different
+        iterations).  The next run() clears the cancel flags."""
+        _lib.check(self.L, self.L.cmc_batch_cancel(self.plan))
+
     def graph(self, nburn=0, niter=0, itr0=0):
         """Capture one chunk (memsets + one persistent launch per size class)
         as a CUDA graph; replaying it runs the chunk again (recording main

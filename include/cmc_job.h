@@ -19,8 +19,9 @@ enum cmc_status {
   CMC_ERR_MODEL = 4,      /* the model reported an error (e.g. bad imodel)    */
   CMC_ERR_NOMEM = 5,      /* device allocation failed                         */
   CMC_ERR_UNSUPPORTED = 6, /* no kernel configuration fits these sizes        */
-  CMC_ERR_TIMEOUT = 7     /* a wait between the CTAs of a spread-layout sweep
+  CMC_ERR_TIMEOUT = 7,    /* a wait between the CTAs of a spread-layout sweep
                              ran out (cmc_set_layout)                         */
+  CMC_ERR_CANCELLED = 8   /* the batch was cancelled (cmc_batch_cancel)      */
 };
 
 enum cmc_prop_mode {

@@ -170,6 +170,16 @@ int cmc_batch_info(void *plan, int cls, int *R, int *G, int *T, int *phasor, int
 int cmc_batch_run_class(void *plan, int cls, int do_init, int nburn, int niter, int itr0,
                         void *stream);
 int cmc_batch_set_class(void *plan, int cls, int R, int T, int phasor, void *stream);
+/* Cancel the plan's running batch launches: callable from any host thread
+ * while cmc_batch_run's launches run on their stream (a cancel that lands
+ * before the run's first memset has executed is cleared by it).  A cluster takes no further (fit, sequence)
+ * item, and one in the middle of an item stops after the exchange of its
+ * current iteration with its state and records written back; every job of
+ * the plan gets CMC_ERR_CANCELLED in its status word (the jobs are left at
+ * different iterations).  The next cmc_batch_run clears the cancel flags;
+ * the status words stay until the caller resets them.  No reference
+ * counterpart (the reference has no batches). */
+int cmc_batch_cancel(void *plan);
 void cmc_batch_free(void *plan);
 
 /* Bytes of library scratch (packed data of the built-in fast models) that

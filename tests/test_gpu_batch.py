@@ -160,3 +160,47 @@ def test_plugin_model_batch_finds_the_rosenbrock_minimum():
         x = s["pout"][:, 0].reshape(4, -1)[:, i].astype(np.float64)
         f = np.sum(100 * (x[1:] - x[:-1] ** 2) ** 2 + (1 - x[:-1]) ** 2)
         assert f < 0.02 and np.all(np.abs(x - 1.0) < 0.2), (x, f)
+
+
+def test_batch_cancel_stops_a_running_batch():
+    """cmc_batch_cancel from the host while a long burn-in runs: the launch
+    ends early (no further items, running ones stop at their next
+    exchange), every job reports CMC_ERR_CANCELLED, the fits' step counters
+    stopped part-way, and the next run (status words reset) runs normally."""
+    import time
+    import torch
+    fits = synth.sgra_batch(nfits=16, seed=9, nseq=8, nbeta=16, nburn=0, niter=0)
+    jobs = [DeviceJob.from_workload(w, niter_total=1, seed=40 + i) for i, w in enumerate(fits)]
+    batch = BatchJob(jobs)
+    batch.run(0, 0, do_init=True)
+    batch.check()
+    t0 = time.perf_counter()
+    batch.run(5, 0)
+    batch.check()
+    per_iter = (time.perf_counter() - t0) / 5
+    n = max(50, int(4.0 / per_iter))          # about 4 s uncancelled
+    t0 = time.perf_counter()
+    batch.run(n, 0)
+    time.sleep(0.3)
+    batch.cancel()
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    assert elapsed < 0.5 * n * per_iter, (elapsed, n * per_iter)
+    for j in jobs:
+        with pytest.raises(_lib.McmcError) as err:
+            j.check()
+        assert err.value.code == _lib.CMC_ERR_CANCELLED
+    # n_cnt [nprm][nbeta][nseq] starts at 1 and counts each parameter's
+    # burn-in proposals: iterations done = (sum over parameters - nprm) / nprm
+    # (5 + n uncancelled).  Small fits may finish before the cancel lands;
+    # the batch as a whole stopped part-way, some of its sequences in the
+    # middle of their burn-in and no fit ran past its schedule
+    nprm = fits[0].nprm
+    done = np.array([(j.to_numpy(("n_cnt",))["n_cnt"].sum(axis=0) - nprm).mean() / nprm
+                     for j in jobs])
+    assert done.sum() < 0.9 * len(jobs) * (5 + n), done
+    assert np.all(done <= 5 + n) and np.any((done > 5) & (done < 5 + n)), done
+    for j in jobs:
+        j.t["status"].zero_()
+    batch.run(2, 0)
+    batch.check()
