@@ -71,7 +71,8 @@ CALC_MODEL_ARGS = [_fp, _ip, _fp, _fp] + [C.c_int] * 8
 EXPORTS = ("mcmc_cuda", "mcmc_cuda_v2", "calc_modchi2", "calc_modchi2_v2", "calc_model",
            "calc_model_v2", "cmc_last_error", "cmc_model_name", "cmc_abi_version",
            "cmc_sizeof_job", "cmc_reset_gpu", "cmc_work_bytes", "cmc_run", "cmc_eval",
-           "cmc_query_config", "cmc_set_config", "cmc_set_layout", "cmc_batch_work_bytes",
+           "cmc_query_config", "cmc_set_config", "cmc_set_layout", "cmc_set_spread",
+           "cmc_query_spread", "cmc_batch_work_bytes",
            "cmc_batch_prepare",
            "cmc_batch_run", "cmc_batch_info", "cmc_batch_free", "cmc_batch_run_class",
            "cmc_batch_cancel",
@@ -109,6 +110,10 @@ def _declare(L):
     L.cmc_set_config.restype = None
     L.cmc_set_layout.argtypes = [C.c_int]
     L.cmc_set_layout.restype = None
+    L.cmc_set_spread.argtypes = [C.c_int, C.c_int]
+    L.cmc_set_spread.restype = None
+    L.cmc_query_spread.argtypes = [C.POINTER(CmcJob), _ip, _ip]
+    L.cmc_query_spread.restype = C.c_int
     L.cmc_batch_work_bytes.argtypes = [C.POINTER(CmcJob), C.c_int]
     L.cmc_batch_work_bytes.restype = C.c_size_t
     L.cmc_batch_prepare.argtypes = [C.POINTER(CmcJob), C.c_int, C.c_void_p, C.c_size_t,

@@ -183,6 +183,17 @@ __host__ __device__ inline int spread_cta_of(int nrep, int N, int f)
   return f < big ? f / (q + 1) : rem + (f - big) / q;
 }
 
+// Sequence group g of ngroups: sequences [seq0, seq0 + n), the first
+// nseq % ngroups groups one sequence larger.  A spread launch runs its groups
+// one after the other on all of its CTAs (only one group's phase regions in
+// use at a time).
+__host__ __device__ inline void spread_group(int nseq, int ngroups, int g, int &seq0, int &n)
+{
+  const int q = nseq / ngroups, rem = nseq % ngroups;
+  n = q + (g < rem ? 1 : 0);
+  seq0 = g * q + (g < rem ? g : rem);
+}
+
 // Global-memory exchange area of a spread launch (in job.work after the
 // model's scratch; spread_ctl_bytes).  The per-iteration buffers are double
 // buffered by iteration parity: a CTA rewrites a buffer two iterations later,
@@ -198,6 +209,7 @@ struct SpreadCtl {
   int hold;      // test hook: the owner of this sequence never completes its
                  // exchange, so that every wait runs out (-1: none; set from
                  // the environment variable CMC_SPREAD_HOLD_SEQ)
+  int ngroups;   // sequence groups run one after the other (spread_group)
 };
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -227,6 +239,7 @@ __host__ __device__ inline SpreadCtl spread_ctl_at(unsigned char *base, int nseq
   c.xperm = reinterpret_cast<int *>(base + o); o += align256(4 * 2 * nrep);
   c.xchi = reinterpret_cast<float *>(base + o);
   c.hold = -1;
+  c.ngroups = 1;
   return c;
 }
 

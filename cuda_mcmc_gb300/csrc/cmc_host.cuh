@@ -52,6 +52,7 @@ inline int cuda_fail(cudaError_t e, const char *what)
 struct Override {
   int R = 0, T = 0, phasor = -1;
   int layout = 0;   // 0 = automatic, 1 = cluster layout, 2 = spread layout
+  int groups = 0, blocks = 0;   // spread layout: sequence groups and CTAs (0 = automatic)
 };
 inline Override &override_cfg()
 {
@@ -281,6 +282,8 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
   // in the cluster ranking's order.
   const int sms = sm_count();
   const int nrep = j.nbeta * j.nseq;
+  const int Gfix = ov.groups ? ov.groups : env_int("CUDA_MCMC_GROUPS", 0);
+  const int Nfix = ov.blocks ? ov.blocks : env_int("CUDA_MCMC_BLOCKS", 0);
   int per_sm_c = 0, load_c = 1 << 30;
   if (found) {
     const int wave = std::min(j.nseq, out.clusters_per_wave);
@@ -295,7 +298,6 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
     bool found_s = false;
     for (int R = 1; R <= std::min(Model::kMaxR, j.nbeta); ++R) {
       if (Rfix && R != Rfix) continue;
-      const int N = (nrep + R - 1) / R;
       const int Ts[] = {64, 128, 256};
       for (int T : Ts) {
         if (Tfix && T != Tfix) continue;
@@ -304,8 +306,7 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
         for (int ph = 2; ph >= 0; --ph) {
           if (Pfix >= 0 && ph != Pfix) continue;
           if (spread_auto && ph != out.phasor) continue;
-          if (ph == 2 && (!global_phases_ok<Model>(pk) || N * R > j.nbeta * j.nseq + Model::kMaxR))
-            continue;
+          if (ph == 2 && !global_phases_ok<Model>(pk)) continue;
           typename Model::Packed q = pk;
           q.phasor = ph;
           if (!spread_ok<Model>(j, q)) continue;
@@ -314,9 +315,36 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
           const int cap = dispatch_spread_R<Model>(R, [&](auto rc) {
             return spread_capacity<Model, decltype(rc)::value>(T, smem);
           });
-          if (cap <= 0 || N > cap || N > nrep) continue;
+          if (cap <= 0) continue;
+          // Sequence groups, run one after the other by the same CTAs: the
+          // fewest whose largest group fits the resident CTAs at R replicas
+          // each and, with phases in global memory, whose largest group's
+          // corner phases fit the L2 budget.
+          double per_seq = 0.0;
+          if constexpr (Model::kGlobalPhases) {
+            if (ph == 2) {
+              const int corners =
+                  (q.ncph > 0 && q.npass >= 2) ? std::min(q.npts, 3 * q.ncph) : 0;
+              per_seq = (double)j.nbeta * corners * 4.0;
+            }
+          }
+          auto fits = [&](int g) {
+            const int smax = (j.nseq + g - 1) / g;
+            return (j.nbeta * smax + R - 1) / R <= cap && (double)smax * per_seq <= l2_budget;
+          };
+          int ng = Gfix ? std::min(Gfix, j.nseq) : 1;
+          while (!Gfix && ng < j.nseq && !fits(ng)) ++ng;
+          // CTAs: the fewest that hold the largest group at R per CTA (every
+          // slot is evaluated, used or not), at most one per replica of the
+          // smallest group
+          const int rep_max = j.nbeta * ((j.nseq + ng - 1) / ng);
+          const int rep_min = j.nbeta * (j.nseq / ng);
+          const int Nlo = (rep_max + R - 1) / R;
+          const int N = Nfix ? Nfix : Nlo;
+          if (N < Nlo || N > std::min(cap, rep_min)) continue;
+          if (ph == 2 && N * R > nrep + Model::kMaxR) continue;
           const int per_sm = (N + sms - 1) / sms;
-          const int load = R * per_sm;
+          const int load = ng * R * per_sm;
           if (spread_auto && (load >= load_c || per_sm < per_sm_c)) continue;
           const int tpr = T / R;
           const int shape_rank = (tpr >= 32 && tpr < 64) ? 0 : (tpr >= 16 && tpr < 128) ? 1 : 2;
@@ -329,6 +357,7 @@ int pick_sweep_config(const cmc_job &j, typename Model::Packed &pk, LaunchCfg &o
             bs.clusters_per_wave = N;
             bs.spread = 1;
             bs.nblocks = N;
+            bs.groups = ng;
             found_s = true;
           }
         }

@@ -17,6 +17,7 @@ struct LaunchCfg {
   size_t smem = 0;
   int spread = 0;    // 1: spread layout (cooperative launch of nblocks CTAs, G = 0)
   int nblocks = 0;
+  int groups = 1;    // spread layout: sequence groups run one after the other
 };
 
 // Clusters of G CTAs (T threads, smem bytes) that can be resident at once;

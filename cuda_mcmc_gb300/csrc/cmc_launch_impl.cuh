@@ -170,6 +170,7 @@ int launch_spread(const cmc_job &j, const typename Model::Packed &pk, const Laun
     return fail(CMC_ERR_CUDA, std::string("spread counters: ") + cudaGetErrorString(e));
   SpreadCtl x = spread_ctl_at(static_cast<unsigned char *>(ctl), j.nseq, j.nbeta, j.nptot);
   if (const char *h = std::getenv("CMC_SPREAD_HOLD_SEQ")) x.hold = std::atoi(h);   // test hook
+  x.ngroups = c.groups;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

@@ -58,14 +58,16 @@ struct SpreadLayout {
   __device__ __forceinline__ int ph_region(int) const { return region0; }
 };
 
-// CTA b of N spreading nseq sequences of nbeta replicas.
-__device__ __forceinline__ SpreadLayout make_spread_layout(int nbeta, int nseq, int N, int b,
-                                                           int region0)
+// CTA b of N spreading the nseq sequences from seq0 on (nbeta replicas each);
+// replica and sequence indices are the job's.
+__device__ __forceinline__ SpreadLayout make_spread_layout(int nbeta, int seq0, int nseq, int N,
+                                                           int b, int region0)
 {
   const int nrep = nbeta * nseq;
   SpreadLayout lay;
   int start = 0;
   spread_range(nrep, N, b, start, lay.cnt);
+  start += seq0 * nbeta;
   lay.nbeta = nbeta;
   lay.gstart = start;
   lay.seq_lo = start / nbeta;
@@ -79,7 +81,8 @@ __device__ __forceinline__ SpreadLayout make_spread_layout(int nbeta, int nseq, 
     lay.own_r = lay.seq_hi * nbeta - start;
   }
   lay.own_ncta = 0;
-  if (lay.own >= 0) lay.own_ncta = spread_cta_of(nrep, N, lay.own * nbeta + nbeta - 1) - b + 1;
+  if (lay.own >= 0)
+    lay.own_ncta = spread_cta_of(nrep, N, (lay.own - seq0) * nbeta + nbeta - 1) - b + 1;
   lay.region0 = region0;
   return lay;
 }
@@ -818,19 +821,33 @@ sweep_kernel(const cmc_job job, const typename Model::Packed pk)
   sweep_body<Model, R>(job, pk);
 }
 
-// One cooperative launch of N = gridDim.x CTAs in the spread layout.  The
-// host checks that the N CTAs are resident at once and that nbeta <= 32,
-// N <= nrep and ceil(nrep / N) <= R <= nbeta (every CTA's count fits its R
-// slots, and a CTA spans at most two sequences); with phases in global
-// memory, that the job's phase area holds N*R regions.
+// One cooperative launch of N = gridDim.x CTAs in the spread layout, over
+// ctl.ngroups sequence groups in turn (the sequences' chains are independent,
+// so the grouping changes no result; it bounds the phase regions in use).
+// The host checks that the N CTAs are resident at once and that nbeta <= 32,
+// N <= every group's nrep and ceil(nrep / N) <= R <= nbeta for the largest
+// (every CTA's count fits its R slots, and a CTA spans at most two
+// sequences); with phases in global memory, that the job's phase area holds
+// N*R regions.
 template <class Model, int R>
 __device__ __forceinline__ void spread_body(const cmc_job &job, const typename Model::Packed &pk,
                                             const SpreadCtl &ctl)
 {
   extern __shared__ __align__(16) unsigned char smem[];
-  const SpreadLayout lay = make_spread_layout(job.nbeta, job.nseq, (int)gridDim.x,
-                                              (int)blockIdx.x, (int)blockIdx.x * R);
-  run_replicas<Model, R>(job, pk, lay, ctl, nullptr, smem);
+  __shared__ int s_abort;
+  for (int g = 0; g < ctl.ngroups; ++g) {
+    // a group starts once every thread of the CTA is done with the last
+    // group's shared memory; none starts after an abort (one reading of the
+    // flag for the whole CTA)
+    if (threadIdx.x == 0) s_abort = (g > 0 && read_flag(ctl.abort) != 0) ? 1 : 0;
+    __syncthreads();
+    if (s_abort) break;
+    int seq0 = 0, n = 0;
+    spread_group(job.nseq, ctl.ngroups, g, seq0, n);
+    const SpreadLayout lay = make_spread_layout(job.nbeta, seq0, n, (int)gridDim.x,
+                                                (int)blockIdx.x, (int)blockIdx.x * R);
+    run_replicas<Model, R>(job, pk, lay, ctl, nullptr, smem);
+  }
 }
 
 template <class Model, int R>

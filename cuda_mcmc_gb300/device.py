@@ -241,28 +241,35 @@ class DeviceJob:
         if self.shape:
             self.L.cmc_set_config(self.shape["R"], self.shape["T"], self.shape["phasor"])
             self.L.cmc_set_layout(int(self.shape.get("layout", 0)))
+            self.L.cmc_set_spread(int(self.shape.get("groups", 0)),
+                                  int(self.shape.get("blocks", 0)))
 
     def _release_shape(self):
         if self.shape:
             self.L.cmc_set_config(0, 0, -1)
             self.L.cmc_set_layout(0)
+            self.L.cmc_set_spread(0, 0)
 
     def config(self):
         """Launch shape used for this job: R, G, T, phasor, smem, clusters/wave
-        and the layout ("cluster", or "spread" with G = 0 and `blocks` CTAs)."""
-        R, G, T, P, W = (C.c_int() for _ in range(5))
+        and the layout ("cluster", or "spread" with G = 0, `blocks` CTAs and
+        `groups` sequence groups)."""
+        R, G, T, P, W, NB, NG = (C.c_int() for _ in range(7))
         sm = C.c_size_t()
         self._force_shape()
         try:
             _lib.check(self.L, self.L.cmc_query_config(C.byref(self.job), C.byref(R), C.byref(G),
                                                        C.byref(T), C.byref(P), C.byref(sm),
                                                        C.byref(W)))
+            _lib.check(self.L, self.L.cmc_query_spread(C.byref(self.job), C.byref(NB),
+                                                       C.byref(NG)))
         finally:
             self._release_shape()
         out = dict(R=R.value, G=G.value, T=T.value, phasor=P.value, smem=sm.value,
                    clusters_per_wave=W.value, layout="cluster" if G.value else "spread")
         if not G.value:
-            out["blocks"] = W.value
+            out["blocks"] = NB.value
+            out["groups"] = NG.value
         return out
 
     # ---- state access ----------------------------------------------------------

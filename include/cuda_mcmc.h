@@ -213,6 +213,21 @@ void cmc_set_config(int R, int T, int phasor);
  * either way.  No reference counterpart. */
 void cmc_set_layout(int layout);
 
+/* Spread layout only: force the number of sequence groups and of CTAs
+ * (0 = automatic).  A spread launch runs its sequences in `groups` groups
+ * (nseq / groups each, the first nseq % groups one more) one after the
+ * other on all of its CTAs, so that with phases in global memory only one
+ * group's phase regions are in use (the automatic choice: the fewest groups
+ * whose corner phases fit in L2).  `blocks` must lie between the fewest CTAs
+ * that hold the largest group at R replicas each and the smallest group's
+ * replica count.  Same chains whatever the grouping.  No reference
+ * counterpart. */
+void cmc_set_spread(int groups, int blocks);
+
+/* The spread layout's CTAs and sequence groups for this job (both 0 in the
+ * cluster layout); returns a cmc_status.  No reference counterpart. */
+int cmc_query_spread(const cmc_job *job, int *blocks, int *groups);
+
 /* libcmc_module.so only; no reference counterpart.  That library is the
  * plugin C-ABI without a model compiled in: its launches take the kernels
  * from a CUDA module file (a cubin or PTX built from a model.cuh with

@@ -147,6 +147,51 @@ def test_spread_global_phases_equal_cluster_layout():
     _same(a, b)
 
 
+GROUPED = {
+    # phases in global memory: 8 sequences in groups of 3, 3 and 2, 14 CTAs
+    "global_3groups": (dict(R=8, T=256, phasor=2, layout=1),
+                       dict(R=7, T=256, phasor=2, layout=2, groups=3)),
+    # phases in shared memory, two groups of 4 on 64 CTAs of 2 replicas each
+    "shared_2groups_N64": (dict(R=4, T=128, phasor=0, layout=1),
+                           dict(R=2, T=128, phasor=0, layout=2, groups=2, blocks=64)),
+}
+
+
+@pytest.mark.parametrize("name", list(GROUPED))
+def test_spread_sequence_groups_equal_cluster_layout(name):
+    """One spread launch running its sequences in groups, one group after the
+    other on all of its CTAs (what bounds the phase regions in use with
+    phases in global memory): the sequences' chains are independent, so every
+    output equals the cluster layout's, bit for bit, over a chunked run."""
+    cl, sp = GROUPED[name]
+    w = synth.sgra(nvis=3000, ncph=900, seed=6, nseq=8, nbeta=32)
+    _, a = _run(w, cl, nburn=3, niter=6, chunks=[(3, 0), (0, 4), (0, 2)])
+    js, b = _run(w, sp, nburn=3, niter=6, chunks=[(3, 0), (0, 4), (0, 2)])
+    cfg = js.config()
+    assert cfg["layout"] == "spread" and cfg["groups"] == sp["groups"], cfg
+    if "blocks" in sp:
+        assert cfg["blocks"] == sp["blocks"]
+    _same(a, b)
+
+
+def test_spread_groups_are_the_automatic_choice_beyond_one_wave():
+    """More replicas than the resident CTAs hold at 7 per CTA (2000 + 600
+    data, 128 x 32 on 152 SMs): the library runs the sequences in two groups
+    of 64 on 293 CTAs (1.106e8 evals/s against the cluster layout's 1.009e8
+    measured on a GB300); the chains are the cluster layout's."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    if sms != 152:
+        pytest.skip("the expected pick is stated for 152 SMs")
+    w = synth.sgra(nvis=2000, ncph=600, seed=3, nseq=128, nbeta=32)
+    job = DeviceJob.from_workload(w, niter_total=2, seed=7)
+    cfg = job.config()
+    assert cfg["layout"] == "spread" and cfg["groups"] == 2 and cfg["R"] == 7, cfg
+    assert cfg["blocks"] == 293
+    _, a = _run(w, dict(R=8, T=256, phasor=cfg["phasor"], layout=1), seed=7, nburn=1, niter=2)
+    _, b = _run(w, None, seed=7, nburn=1, niter=2)
+    _same(a, b)
+
+
 def test_spread_rejects_what_it_cannot_run():
     """Forced onto a job it cannot hold (more than 32 temperatures), the
     spread layout reports no shape instead of running."""
@@ -171,6 +216,31 @@ def test_spread_wait_that_runs_out_reports_timeout(monkeypatch):
     job = DeviceJob.from_workload(w, niter_total=2, seed=5)
     job.shape = shape
     monkeypatch.setenv("CMC_SPREAD_HOLD_SEQ", "0")
+    t0 = time.perf_counter()
+    job.run(2, 2, do_init=True)
+    with pytest.raises(_lib.McmcError) as err:
+        job.check()
+    elapsed = time.perf_counter() - t0
+    monkeypatch.delenv("CMC_SPREAD_HOLD_SEQ")
+    assert err.value.code == _lib.CMC_ERR_TIMEOUT
+    assert elapsed < 30.0
+    _, a = _run(w, dict(R=8, T=128, phasor=0, layout=1), nburn=2, niter=2)
+    _, b = _run(w, shape, nburn=2, niter=2)
+    _same(a, b)
+
+
+def test_spread_timeout_in_a_group_skips_the_later_groups(monkeypatch):
+    """The held sequence in the first of two groups: its waits run out, the
+    CTAs start no later group (the abort flag is read once per CTA before
+    each), and the launch reports CMC_ERR_TIMEOUT; the next launch runs
+    normally."""
+    import time
+    from cuda_mcmc_gb300 import _lib
+    w = synth.sgra(nvis=400, ncph=120, seed=3, nseq=4, nbeta=16)
+    shape = dict(R=4, T=128, phasor=0, layout=2, groups=2)
+    job = DeviceJob.from_workload(w, niter_total=2, seed=5)
+    job.shape = shape
+    monkeypatch.setenv("CMC_SPREAD_HOLD_SEQ", "1")
     t0 = time.perf_counter()
     job.run(2, 2, do_init=True)
     with pytest.raises(_lib.McmcError) as err:
