@@ -417,7 +417,8 @@ def e2e_rate(w, args, steps, warmup):
     h2d = sum(a.nbytes for a in (w.coor, w.dat, w.std2r, w.icoor, w.idat, s["pdescr"], s["ivar"],
                                  s["invar"], s["pmint"], s["pmaxt"], s["tcur"], s["flag"],
                                  s["chi2c"], s["n_acpt"], s["n_exch"], s["n_cnt"], s["n_hist"],
-                                 beta, s["pstp"], s["ptent"], s["ptentn"], s["pcur"]))
+                                 beta, s["pstp"], s["ptent"], s["ptentn"], s["pcur"],
+                                 out[6]))   # rndst goes in as well (src/mcmcjob.cu:724)
     d2h = sum(a.nbytes for a in out[1:]) + sum(
         s[k].nbytes for k in ("tcur", "n_acpt", "n_cnt", "n_exch", "n_hist", "pstp", "ptent",
                               "ptentn", "pcur", "flag", "chi2c"))

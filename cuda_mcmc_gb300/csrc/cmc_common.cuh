@@ -77,10 +77,31 @@ __device__ __forceinline__ float warp_sum(float v)
 // injected stream pair with cursors.
 struct Rng {
   curandStateXORWOW st;
+  unsigned pad;   // bytes 36-39 of the stored 48-byte state (padding before the double)
   const float *u, *n;
   int cu, cn, lu, ln;
   bool inj;
   bool ovf;
+
+  // The stored state, word by word: the fields (d, v[5], the Box-Muller
+  // flags and cached values), then the 4 padding bytes and the cached
+  // double.  The reference runs curand_init on its device copy of the
+  // caller's array and copies the array back, so the padding keeps the
+  // caller's bytes: they are read and written back unchanged here.
+  __device__ void store_state(unsigned char *p) const
+  {
+    unsigned *w = reinterpret_cast<unsigned *>(p);
+    w[0] = st.d;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) w[1 + i] = st.v[i];
+    w[6] = (unsigned)st.boxmuller_flag;
+    w[7] = (unsigned)st.boxmuller_flag_double;
+    w[8] = __float_as_uint(st.boxmuller_extra);
+    w[9] = pad;
+    const unsigned long long e = (unsigned long long)__double_as_longlong(st.boxmuller_extra_double);
+    w[10] = (unsigned)e;
+    w[11] = (unsigned)(e >> 32);
+  }
 
   __device__ float uniform()
   {

@@ -1054,6 +1054,9 @@ int host_mcmc(float *coor, float *dat, float *std2r, int *icoor, int *idat, floa
   CMC_TRY(h2d(j.ptent, ptent, nrep, s));
   CMC_TRY(h2d(j.ptentn, ptentn, nrep, s));
   CMC_TRY(h2d(j.pcur, pcur, nrep * nptot, s));
+  // the generator states go in as well (src/mcmcjob.cu:724): curand_init
+  // rewrites their fields and leaves the padding bytes as the caller's
+  CMC_TRY(h2d(j.rndst, rndst, 48 * nrep, s));
   CMC_CUDA(cudaMemsetAsync(j.status, 0, sizeof(int), s));
 
   CMC_TRY(run_sweep<Model>(j, s));

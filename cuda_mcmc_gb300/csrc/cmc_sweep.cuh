@@ -292,6 +292,7 @@ struct SweepState {
   {
     rng.inj = (job->rng_mode == CMC_RNG_INJECTED);
     rng.ovf = false;
+    rng.pad = 0u;
     rng.u = rng.n = nullptr;
     rng.cu = rng.cn = rng.lu = rng.ln = 0;
     s_k[r] = 0;
@@ -315,15 +316,18 @@ struct SweepState {
       rng.ln = job->inj_ln;
       rng.cu = job->do_init ? 0 : job->inj_cur[2 * ist];
       rng.cn = job->do_init ? 0 : job->inj_cur[2 * ist + 1];
-    } else if (job->do_init) {
-      // the replica's subsequence in the unsharded run (ist when unsharded)
-      const unsigned long long sub =
-          job->nseq_total > 0
-              ? (unsigned long long)ibeta * job->nseq_total + job->seq_offset + iseq
-              : (unsigned long long)ist;
-      curand_init(job->seed, sub, 0ull, &rng.st);
     } else {
-      rng.st = reinterpret_cast<const curandStateXORWOW *>(job->rndst)[ist];
+      rng.pad = reinterpret_cast<const unsigned *>(job->rndst + (size_t)48 * ist)[9];
+      if (job->do_init) {
+        // the replica's subsequence in the unsharded run (ist when unsharded)
+        const unsigned long long sub =
+            job->nseq_total > 0
+                ? (unsigned long long)ibeta * job->nseq_total + job->seq_offset + iseq
+                : (unsigned long long)ist;
+        curand_init(job->seed, sub, 0ull, &rng.st);
+      } else {
+        rng.st = reinterpret_cast<const curandStateXORWOW *>(job->rndst)[ist];
+      }
     }
   }
 
@@ -536,7 +540,7 @@ struct SweepState {
       job->inj_cur[2 * ist] = rng.cu;
       job->inj_cur[2 * ist + 1] = rng.cn;
     } else {
-      reinterpret_cast<curandStateXORWOW *>(job->rndst)[ist] = rng.st;
+      rng.store_state(job->rndst + (size_t)48 * ist);
     }
     if (rng.ovf) set_status(job->status, CMC_ERR_STREAM);
   }

@@ -365,6 +365,46 @@ def test_mcmc_cuda_host_abi_equals_device_api():
     assert np.array_equal(datm, dev["datm"]) and np.array_equal(chi2m, dev["chi2m"])
 
 
+def _host_call(w, seed, rndst):
+    from cuda_mcmc_gb300.device import sampler_defaults
+    s = sampler_defaults(w.pdescr, w.pmint, w.pmaxt, w.nbeta, w.nseq)
+    nrep, nprm = w.nbeta * w.nseq, w.nprm
+    out = dict(pout=np.zeros((nprm, w.nbeta, w.nseq, w.niter), np.float32),
+               tout=np.zeros((w.nbeta, w.nseq, w.niter), np.int32),
+               chi2=np.zeros((w.nseq, w.niter), np.float32),
+               datm=np.zeros(nrep * (w.ndat + w.nvis), np.float32),
+               chi2m=np.zeros((w.nbeta, w.nseq, w.ndat), np.float32), rndst=rndst)
+    mcmc_interf.use_model("sgra")
+    mcmc_interf.mcmcuda(w.coor, w.dat, w.std2r, w.icoor, w.idat, out["datm"], out["chi2m"],
+                        s["pdescr"], s["ivar"], s["invar"], s["ptotal"], s["pmint"], s["pmaxt"],
+                        out["pout"], out["tout"], out["chi2"], s["chi2c"], s["tcur"], s["flag"],
+                        s["n_acpt"], s["n_exch"], s["n_cnt"], s["n_hist"], w.beta(), s["pstp"],
+                        s["ptent"], s["ptentn"], s["pcur"], rndst, np.uint64(seed), w.imodel,
+                        w.coor.size, w.ndat, w.icoor.size, w.idat.size, out["datm"].size,
+                        w.nptot, nprm, 100, w.npass, w.nbeta, w.nseq, w.nburn, w.niter)
+    out.update(s)
+    return out
+
+
+def test_mcmc_cuda_generator_states_are_the_callers_array():
+    """rndst goes to the device and back as in the reference
+    (src/mcmcjob.cu:724, 765): curand_init rewrites each 48-byte XORWOW
+    state's fields in place and leaves its 4 padding bytes (36-39) as the
+    caller's.  The output does not depend on what an earlier call left in
+    the library's device memory pool (an unrelated 64 x 32 call in between)."""
+    w = synth.sgra(nvis=2000, ncph=600, seed=3, nseq=4, nbeta=8, nburn=6, niter=6)
+    a = _host_call(w, 4242, np.zeros((w.nbeta, w.nseq, 48), np.uint8))
+    big = synth.sgra(nvis=2000, ncph=600, seed=3, nseq=64, nbeta=32, nburn=1, niter=2)
+    _host_call(big, 11, np.full((big.nbeta, big.nseq, 48), 0x5C, np.uint8))
+    b = _host_call(w, 4242, np.full((w.nbeta, w.nseq, 48), 0xAB, np.uint8))
+    assert np.all(b["rndst"][..., 36:40] == 0xAB) and np.all(a["rndst"][..., 36:40] == 0)
+    assert np.array_equal(a["rndst"][..., :36], b["rndst"][..., :36])
+    assert np.array_equal(a["rndst"][..., 40:], b["rndst"][..., 40:])
+    for f in ("pout", "tout", "chi2", "datm", "chi2m", "pcur", "chi2c", "n_acpt", "n_exch",
+              "n_cnt", "n_hist", "tcur", "pstp", "flag"):
+        assert np.array_equal(a[f], b[f]), f
+
+
 def test_chunked_run_equals_single_launch():
     w = synth.nlsys(nseq=4, nbeta=8)
     a = DeviceJob.from_workload(w, niter_total=40, seed=5)
