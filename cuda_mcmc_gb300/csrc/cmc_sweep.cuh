@@ -60,8 +60,8 @@ struct SpreadLayout {
 
 // CTA b of N spreading the nseq sequences from seq0 on (nbeta replicas each);
 // replica and sequence indices are the job's.
-__device__ __forceinline__ SpreadLayout make_spread_layout(int nbeta, int seq0, int nseq, int N,
-                                                           int b, int region0)
+__host__ __device__ __forceinline__ SpreadLayout make_spread_layout(int nbeta, int seq0, int nseq,
+                                                                    int N, int b, int region0)
 {
   const int nrep = nbeta * nseq;
   SpreadLayout lay;
