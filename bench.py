@@ -135,13 +135,13 @@ def evals_per_step(w, args):
 # DRAM bytes of one sweep launch of the 2000 vis + 600 closure, 64 x 32 workload:
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of a 16-iteration launch of
 # the library's shape (spread layout, R=7, T=256; 4 burn-in + 12 recorded;
-# 27.0 + 29.2 MB) = a fixed part (state, model data per CTA, final datm /
+# 26.7 + 28.0 MB) = a fixed part (state, model data per CTA, final datm /
 # chi2m rows) plus the records of each main iteration (pout + tout + chi2,
 # 9*32*64*4 + 32*64*4 + 64*4 bytes).
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 16-iteration launch "
-                  "(56.3 MB) scaled to this launch: fixed part + the records of each main "
+                  "(54.7 MB) scaled to this launch: fixed part + the records of each main "
                   "iteration; only for the 2000 vis + 600 closure 64 x 32 workload")
-_TRAFFIC_CAPTURE = 56.3e6
+_TRAFFIC_CAPTURE = 54.7e6
 _TRAFFIC_REC_PER_ITER = 9 * 32 * 64 * 4 + 32 * 64 * 4 + 64 * 4
 
 
