@@ -237,6 +237,11 @@ class DeviceJob:
         if st:
             raise _lib.McmcError(st, "device status %d (see cmc_status in cmc_job.h)" % st)
 
+    def clear_status(self):
+        """Reset the device status word (after an error or a batch cancel was
+        read), so that the job can run again."""
+        self.t["status"].zero_()
+
     def _force_shape(self):
         if self.shape:
             self.L.cmc_set_config(self.shape["R"], self.shape["T"], self.shape["phasor"])
@@ -366,7 +371,8 @@ class BatchJob:
         running one stops after its current iteration's exchange with its
         state and records written back, and every job's status becomes
         CMC_ERR_CANCELLED (its check() raises; the jobs are left at different
-        iterations).  The next run() clears the cancel flags."""
+        iterations).  The next run() clears the cancel flags; clear_status()
+        resets the status words."""
         _lib.check(self.L, self.L.cmc_batch_cancel(self.plan))
 
     def graph(self, nburn=0, niter=0, itr0=0):
@@ -480,6 +486,11 @@ class BatchJob:
     def check(self):
         for j in self.jobs:
             j.check()
+
+    def clear_status(self):
+        """Reset every job's status word (after cancel())."""
+        for j in self.jobs:
+            j.clear_status()
 
     def __del__(self):
         plan = getattr(self, "plan", None)

@@ -200,7 +200,6 @@ def test_batch_cancel_stops_a_running_batch():
                      for j in jobs])
     assert done.sum() < 0.9 * len(jobs) * (5 + n), done
     assert np.all(done <= 5 + n) and np.any((done > 5) & (done < 5 + n)), done
-    for j in jobs:
-        j.t["status"].zero_()
+    batch.clear_status()
     batch.run(2, 0)
     batch.check()
