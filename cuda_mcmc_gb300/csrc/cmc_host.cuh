@@ -47,8 +47,11 @@ inline int cuda_fail(cudaError_t e, const char *what)
     if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
   } while (0)
 
-// Launch-shape override set by cmc_set_config (the autotuner) or the
-// CUDA_MCMC_R / CUDA_MCMC_THREADS environment variables; 0 = automatic.
+// Launch-shape override set by cmc_set_config / cmc_set_layout /
+// cmc_set_spread (the autotuner, tests) or, where those are unset, by the
+// environment variables CUDA_MCMC_R, CUDA_MCMC_THREADS, CUDA_MCMC_PHASOR,
+// CUDA_MCMC_LAYOUT, CUDA_MCMC_GROUPS and CUDA_MCMC_BLOCKS; 0 (phase mode -1)
+// = automatic.
 struct Override {
   int R = 0, T = 0, phasor = -1;
   int layout = 0;   // 0 = automatic, 1 = cluster layout, 2 = spread layout
